@@ -1,0 +1,341 @@
+#!/usr/bin/env python3
+"""Benchmark: binary256 FMA throughput (Gelem/s, bit-exact) on GB300.
+
+Workload (one "step" = one pass of the hot path over one batch):
+    binary256 fused multiply-add d = a*b + c, roundTiesToEven, n = 2^24
+    elements - the fp256 x FMA x RNE cell of the elementwise sweep - over
+    seeded synthetic operands with the sweep's value mix (90% normals with
+    exponents in [-64, 64], 10% specials, exact-cancellation triples).
+    Inputs are 1.5 GiB, larger than L2, so no flush is needed between steps.
+
+value   whole-job Gelem/s with operands resident in HBM (device pointers
+        through cftg_run_device), timed with CUDA events on the launch
+        stream, max over ranks.
+e2e     the same through the reference-facing C ABI (cft_run) with pinned
+        HOST buffers: uploads, kernel and download inside the timed region.
+roofline  the FMA kernel's algorithmic bytes (4 x 32 B an element) per
+        launch over its measured launch time, against the measured HBM copy
+        bandwidth.
+cpu_baseline  the oracle's C restatement of the reference softfloat, on all
+        host cores, over a bounded sample of the same operands.
+
+--impl reference runs the reference path's CPU arithmetic (the oracle port;
+the reference library itself cannot be built on the GPU host) on the host
+cores and prints the same line with "impl": "reference".
+
+Multi-GPU: one process per GPU (torchrun); each rank runs its own 2^24
+elements (the path shards by element with no exchange but an OR of the
+flag word), "scaling": "weak", value = all ranks' elements / slowest rank.
+"""
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT / "cft-fp256_gb300"))
+
+METRIC = "fp256/fp128 FMA Gelem/s bit-exact (plain vs batched); mixed-load p50/p99 latency"
+N_DEFAULT = 1 << 24
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        j = json.loads(p.read_text())
+        return float(j["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index),
+                 "--query-gpu=clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,"
+                 "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 6:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[2:6]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_baseline(fmt, a, b, c, seconds=12.0, per_call=2048):
+    """The oracle (C restatement of the reference softfloat) on all host
+    cores: threads each run chunks of `per_call` elements until the time
+    budget is spent. ctypes releases the GIL inside the call."""
+    sys.path.insert(0, str(ROOT / "tests"))
+    import oracle_lib
+    o = oracle_lib.Oracle()
+    threads = os.cpu_count() or 1
+    n = a.shape[0]
+    done = [0] * threads
+    stop = time.perf_counter() + seconds
+
+    def worker(t):
+        L = o.L
+        d = np.zeros((per_call, a.shape[1]), np.uint32)
+        acc = ctypes.c_uint32()
+        k = t
+        while time.perf_counter() < stop:
+            s = (k * per_call) % (n - per_call)
+            L.sfp_run(0, fmt, 0, 0, a[s:].ctypes.data, b[s:].ctypes.data, c[s:].ctypes.data,
+                      d.ctypes.data, per_call, 0, None, ctypes.byref(acc))
+            done[t] += per_call
+            k += threads
+    t0 = time.perf_counter()
+    th = [threading.Thread(target=worker, args=(i,)) for i in range(threads)]
+    for x in th:
+        x.start()
+    for x in th:
+        x.join()
+    dt = time.perf_counter() - t0
+    return sum(done) / dt, threads, sum(done), dt
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def run_reference(args):
+    ws, rank, _ = dist_init()
+    if rank != 0:
+        return
+    fmt = 3
+    a, b, c = (np.ascontiguousarray(x) for x in
+               __import__("cftgb.workload", fromlist=["x"]).gen_operands(fmt, 1 << 16, 1))
+    per_step = []
+    for _ in range(args.warmup):
+        cpu_baseline(fmt, a, b, c, seconds=0.5)
+    total, thr = 0, 1
+    t_all = 0.0
+    for _ in range(args.steps):
+        rate, thr, cnt, dt = cpu_baseline(fmt, a, b, c, seconds=2.0)
+        per_step.append(dt)
+        total += cnt
+        t_all += dt
+    value = total / t_all / 1e9
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "Gelem/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000 * t_all / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u32-limb binary256", "data": "synthetic",
+        "config": {"workload": "binary256 FMA RNE, seeded operand mix (90% normals, 10% specials, "
+                               "cancellation triples)", "elements_per_step": "2 s of host work",
+                   "parallelism": "host threads"},
+        "cpu_baseline": {"value": value, "unit": "Gelem/s", "cores": thr, "kind": "port",
+                         "sample": "2 s per step of 2048-element calls over 65,536 operands"},
+        "e2e": {"value": value, "unit": "Gelem/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=N_DEFAULT)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    import cftgb
+    from cftgb import workload as wl
+
+    ws, rank, local = dist_init()
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev_index = local if ws > 1 else 0
+    torch.cuda.set_device(dev_index)
+    h = cftgb.open_device(f"cuda:{dev_index}")
+    L = cftgb.lib()
+    n = args.n
+    fmt = 3
+    a, b, c = wl.gen_operands(fmt, n, 1 + rank)
+    W = wl.words(fmt)
+    ta, tb, tc = (torch.from_numpy(x.view(np.int32)).cuda() for x in (a, b, c))
+    td = torch.zeros_like(ta)
+    tf = torch.zeros(1, dtype=torch.int32, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    def launch(fmt_, A, B, C, D, nn):
+        st = L.cftg_run_device(h, 0, 0, fmt_, 0, A.data_ptr(), B.data_ptr(), C.data_ptr(),
+                               D.data_ptr(), nn, 0, None, tf.data_ptr(), stream.cuda_stream)
+        if st:
+            cftgb._lib.check(st, "cftg_run_device")
+
+    def barrier():
+        if ws > 1:
+            torch.distributed.barrier()
+
+    # ---- device-resident leg (value, roofline) ----
+    for _ in range(max(3, args.warmup)):
+        launch(fmt, ta, tb, tc, td, n)
+    torch.cuda.synchronize()
+    barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks(dev_index) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            launch(fmt, ta, tb, tc, td, n)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    barrier()
+    ms = e0.elapsed_time(e1)
+    if ws > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    sec = ms / 1e3
+    value = ws * n * args.steps / sec / 1e9
+    per_launch = sec / args.steps
+    hbm_peak, peak_kind = peaks()
+    alg_bytes = 4 * 32 * n
+    achieved = alg_bytes / per_launch / 1e9
+
+    # correctness of what was timed: a sample against the oracle
+    sample_ok = None
+    if rank == 0 and not args.no_cpu:
+        sys.path.insert(0, str(ROOT / "tests"))
+        import oracle_lib
+        o = oracle_lib.Oracle()
+        got = td[:8192].cpu().numpy().view(np.uint32)
+        rd, _, _ = o.run(0, fmt, 0, 0, a[:8192], b[:8192], c[:8192])
+        sample_ok = bool(np.array_equal(got, rd))
+
+    # fp128 FMA on the same terms (the metric's second format)
+    a2, b2, c2 = wl.gen_operands(2, n, 7 + rank)
+    t2 = [torch.from_numpy(x.view(np.int32)).cuda() for x in (a2, b2, c2)]
+    td2 = torch.zeros_like(t2[0])
+    for _ in range(3):
+        launch(2, t2[0], t2[1], t2[2], td2, n)
+    torch.cuda.synchronize()
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record(stream)
+    for _ in range(args.steps):
+        launch(2, t2[0], t2[1], t2[2], td2, n)
+    f1.record(stream)
+    torch.cuda.synchronize()
+    fp128_value = n * args.steps / (f0.elapsed_time(f1) / 1e3) / 1e9
+    del t2, td2
+
+    # ---- end-to-end leg through cft_run with pinned host buffers ----
+    ha, hb, hc = (torch.from_numpy(x.view(np.int32)).pin_memory() for x in (a, b, c))
+    hd = torch.zeros_like(ha).pin_memory()
+    fl = ctypes.c_uint32()
+    for _ in range(max(2, args.warmup // 2)):
+        L.cft_run(h, 0, fmt, 0, ha.data_ptr(), hb.data_ptr(), hc.data_ptr(), hd.data_ptr(), n,
+                  ctypes.byref(fl), None)
+    e2e_steps = max(3, args.steps // 4)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        st = L.cft_run(h, 0, fmt, 0, ha.data_ptr(), hb.data_ptr(), hc.data_ptr(), hd.data_ptr(),
+                       n, ctypes.byref(fl), None)
+        cftgb._lib.check(st, "cft_run")
+    e2e_sec = time.perf_counter() - t0
+    if ws > 1:
+        t = torch.tensor([e2e_sec], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_sec = float(t.item())
+    e2e_value = ws * n * e2e_steps / e2e_sec / 1e9
+    e2e_ok = bool(np.array_equal(hd[:4096].numpy().view(np.uint32),
+                                 td[:4096].cpu().numpy().view(np.uint32)))
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        rate, thr, cnt, dt = cpu_baseline(fmt, a[:1 << 16], b[:1 << 16], c[:1 << 16])
+        cpu = {"value": rate / 1e9, "unit": "Gelem/s", "cores": thr, "kind": "port",
+               "sample": f"{cnt} elements ({dt:.1f} s) of the same operands in 2048-element calls"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "Gelem/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "u32-limb binary256", "data": "synthetic",
+            "config": {"workload": "binary256 FMA RNE, n=2^24 per GPU, seeded operand mix (90% "
+                                   "normals exp in [-64,64], 10% specials, cancellation triples)",
+                       "elements_per_gpu": n, "l2": "inputs 1.5 GiB > L2, no flush",
+                       "parallelism": f"replicas x{ws} (element shards)"},
+            "e2e": {"value": e2e_value, "unit": "Gelem/s", "h2d_bytes_per_step": 3 * 32 * n,
+                    "d2h_bytes_per_step": 32 * n + 8, "path": "cft_run, pinned host buffers",
+                    "steps": e2e_steps},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                         "frac": achieved / hbm_peak, "traffic": None,
+                         "peak_source": peak_kind,
+                         "note": "integer-pipe bound kernel: algorithmic 128 B/element"},
+            "cpu_baseline": cpu,
+            "gpu_launches": args.steps,
+            "clocks": clk.summary(),
+            "fp128_fma_gelem_s": fp128_value,
+            "sample_bit_exact": sample_ok, "e2e_matches_device": e2e_ok,
+        }
+        print(json.dumps(line))
+    cftgb.close_device(h)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

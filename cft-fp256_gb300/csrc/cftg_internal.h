@@ -1,0 +1,74 @@
+// cftg_internal.h - what the host layer (api.cpp, program.cpp) and the
+// kernels (elem.cu, seq.cu, queue.cu) share. Nothing here is exported.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace cftg {
+
+// Kinds of elementwise work one launch does.
+enum ElemKind : int {
+    K_FMA = 0, K_ADD = 1, K_SUB = 2, K_MUL = 3,   // the FMA core, steered
+    K_DIV = 4, K_SQRT = 5,                        // the contract's div/sqrt
+    K_SIMPLE = 6                                  // every other opcode
+};
+
+inline int elem_kind_of_op(int op)
+{
+    return (op >= 0 && op <= 3) ? op : K_SIMPLE;
+}
+
+// One elementwise launch over device memory. Every operand pointer is a
+// device pointer; a NULL operand reads +0 (the reference's loop loads a
+// zeroed element for an operand the caller did not pass).
+struct ElemLaunch {
+    int fmt = 0, kind = 0, op = 0, rnd = 0;
+    const void *a = nullptr, *b = nullptr, *c = nullptr;
+    void *d = nullptr;
+    uint32_t scalar_mask = 0;                 // bit r: operand r is element 0 for all i
+    const uint32_t *ia = nullptr, *ib = nullptr, *ic = nullptr;   // index tables
+    size_t n = 0;
+    uint32_t *flags = nullptr;                // device word, ORed into
+    uint8_t *lane_flags = nullptr;            // optional, n bytes
+};
+
+// Launch on `stream`; returns the launch status.
+cudaError_t launch_elem(const ElemLaunch &L, cudaStream_t stream);
+
+// The kernels' dimensions for a given launch (used by the queue autotuner).
+int sm_count();
+
+// ---- the sequencer ------------------------------------------------------
+
+// A loaded program as the GPU executor reads it (built by program.cpp).
+struct SeqProgram {
+    int fmt = 0;
+    uint32_t n_insns = 0, n_consts = 0, max_deposits = 0, flags = 0;
+    uint32_t n_scratch_in = 0, n_scratch_out = 0;
+    uint32_t scratch_used = 0, scratch_depth = 256, scratch_log2 = 8;
+    int scratch_active = 0;
+    uint32_t reach = 0;                       // slots a lane's scratch clears
+    const uint64_t *d_insns = nullptr;        // device copy of the instruction words
+    const void *d_consts = nullptr;           // device constants (or the run's bank)
+    const int32_t *d_endrep = nullptr;        // REPEAT pc -> matching ENDREP pc
+};
+
+struct SeqLaunch {
+    SeqProgram P;
+    size_t n = 0;
+    const void *a = nullptr, *b = nullptr, *c = nullptr;
+    const uint32_t *ia = nullptr, *ib = nullptr, *ic = nullptr, *isi = nullptr;
+    const void *scratch_in = nullptr;
+    void *scratch_out = nullptr;
+    void *deposits = nullptr;
+    uint32_t *counts = nullptr;
+    const uint8_t *lane_mask = nullptr;
+    uint8_t *lane_flags = nullptr;
+    void *scratch = nullptr;                  // n * reach * esz device bytes (or null)
+    uint32_t *word = nullptr;                 // [0] flags, [1] status, [2] error
+};
+
+cudaError_t launch_seq(const SeqLaunch &L, cudaStream_t stream);
+
+}  // namespace cftg

@@ -1,0 +1,231 @@
+// sf_words.cuh - fixed-width unsigned integers held in registers.
+//
+// Every value is an array of N 32-bit words, little-endian, with N known at
+// compile time so that the arrays stay in registers after unrolling. All
+// variable shifts are select networks (one stage per bit of the word count)
+// plus a funnel shift, so no array is ever indexed by a run-time value.
+#pragma once
+#include <cstdint>
+
+#define SFD __device__ __forceinline__
+
+namespace sfw {
+
+template <int N>
+SFD void zero(uint32_t (&x)[N])
+{
+#pragma unroll
+    for (int i = 0; i < N; i++) x[i] = 0u;
+}
+
+template <int N>
+SFD bool is_zero(const uint32_t (&x)[N])
+{
+    uint32_t o = 0u;
+#pragma unroll
+    for (int i = 0; i < N; i++) o |= x[i];
+    return o == 0u;
+}
+
+// Number of significant bits (0 for zero).
+template <int N>
+SFD int bitlen(const uint32_t (&x)[N])
+{
+    int L = 0;
+#pragma unroll
+    for (int i = 0; i < N; i++)
+        if (x[i]) L = 32 * i + 32 - __clz(x[i]);
+    return L;
+}
+
+// x <<= s for 0 <= s < 32N, zero fill.
+template <int N>
+SFD void shl(uint32_t (&x)[N], int s)
+{
+    const int ws = s >> 5, bs = s & 31;
+#pragma unroll
+    for (int b = 16; b >= 1; b >>= 1) {
+        if (b < N) {
+            const bool take = (ws & b) != 0;
+#pragma unroll
+            for (int i = N - 1; i >= 0; i--)
+                x[i] = take ? (i - b >= 0 ? x[i - b] : 0u) : x[i];
+        }
+    }
+#pragma unroll
+    for (int i = N - 1; i >= 1; i--) x[i] = __funnelshift_l(x[i - 1], x[i], bs);
+    x[0] <<= bs;
+}
+
+// x >>= s with every bit shifted out ORed into bit 0 ("jamming").
+// Any s >= 0; s >= 32N leaves only the jam.
+template <int N>
+SFD void shr_jam(uint32_t (&x)[N], int s)
+{
+    if (s <= 0) return;
+    if (s >= 32 * N) {
+        const bool any = !is_zero(x);
+        zero(x);
+        x[0] = any ? 1u : 0u;
+        return;
+    }
+    const int ws = s >> 5, bs = s & 31;
+    uint32_t st = 0u;
+#pragma unroll
+    for (int i = 0; i < N; i++) {
+        const uint32_t m = (i < ws) ? 0xFFFFFFFFu : (i == ws ? ((1u << bs) - 1u) : 0u);
+        st |= x[i] & m;
+    }
+#pragma unroll
+    for (int b = 16; b >= 1; b >>= 1) {
+        if (b < N) {
+            const bool take = (ws & b) != 0;
+#pragma unroll
+            for (int i = 0; i < N; i++)
+                x[i] = take ? (i + b < N ? x[i + b] : 0u) : x[i];
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < N - 1; i++) x[i] = __funnelshift_r(x[i], x[i + 1], bs);
+    x[N - 1] >>= bs;
+    x[0] |= (st != 0u) ? 1u : 0u;
+}
+
+// x >>= s for 0 <= s < 32N, logical (no jam).
+template <int N>
+SFD void shr(uint32_t (&x)[N], int s)
+{
+    const int ws = s >> 5, bs = s & 31;
+#pragma unroll
+    for (int b = 16; b >= 1; b >>= 1) {
+        if (b < N) {
+            const bool take = (ws & b) != 0;
+#pragma unroll
+            for (int i = 0; i < N; i++)
+                x[i] = take ? (i + b < N ? x[i + b] : 0u) : x[i];
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < N - 1; i++) x[i] = __funnelshift_r(x[i], x[i + 1], bs);
+    x[N - 1] >>= bs;
+}
+
+// x >>= s for a compile-time 0 <= S < 32N (no jam).
+template <int S, int N>
+SFD void shr_const(uint32_t (&x)[N])
+{
+    constexpr int ws = S >> 5, bs = S & 31;
+#pragma unroll
+    for (int i = 0; i < N; i++) {
+        const uint32_t lo = (i + ws < N) ? x[i + ws] : 0u;
+        const uint32_t hi = (i + ws + 1 < N) ? x[i + ws + 1] : 0u;
+        x[i] = bs ? __funnelshift_r(lo, hi, bs) : lo;
+    }
+}
+
+// r = a + b, returns the carry out.
+template <int N>
+SFD uint32_t add(uint32_t (&r)[N], const uint32_t (&a)[N], const uint32_t (&b)[N])
+{
+    uint32_t c = 0u;
+#pragma unroll
+    for (int i = 0; i < N; i++) {
+        const uint64_t t = (uint64_t)a[i] + b[i] + c;
+        r[i] = (uint32_t)t;
+        c = (uint32_t)(t >> 32);
+    }
+    return c;
+}
+
+// r = a - b, returns the borrow out (1 when a < b).
+template <int N>
+SFD uint32_t sub(uint32_t (&r)[N], const uint32_t (&a)[N], const uint32_t (&b)[N])
+{
+    uint32_t br = 0u;
+#pragma unroll
+    for (int i = 0; i < N; i++) {
+        const uint64_t t = (uint64_t)a[i] - b[i] - br;
+        r[i] = (uint32_t)t;
+        br = (uint32_t)(t >> 63);
+    }
+    return br;
+}
+
+// x = -x modulo 2^(32N)
+template <int N>
+SFD void neg(uint32_t (&x)[N])
+{
+    uint32_t c = 1u;
+#pragma unroll
+    for (int i = 0; i < N; i++) {
+        const uint64_t t = (uint64_t)(~x[i]) + c;
+        x[i] = (uint32_t)t;
+        c = (uint32_t)(t >> 32);
+    }
+}
+
+// x += 1, returns the carry out
+template <int N>
+SFD uint32_t inc(uint32_t (&x)[N])
+{
+    uint32_t c = 1u;
+#pragma unroll
+    for (int i = 0; i < N; i++) {
+        const uint64_t t = (uint64_t)x[i] + c;
+        x[i] = (uint32_t)t;
+        c = (uint32_t)(t >> 32);
+    }
+    return c;
+}
+
+// -1, 0, 1
+template <int N>
+SFD int cmp(const uint32_t (&a)[N], const uint32_t (&b)[N])
+{
+    int r = 0;
+#pragma unroll
+    for (int i = 0; i < N; i++)
+        if (a[i] != b[i]) r = a[i] < b[i] ? -1 : 1;
+    return r;
+}
+
+// r (2N words) = a * b, schoolbook with 64-bit partial products.
+template <int N>
+SFD void mul(uint32_t (&r)[2 * N], const uint32_t (&a)[N], const uint32_t (&b)[N])
+{
+#pragma unroll
+    for (int i = 0; i < 2 * N; i++) r[i] = 0u;
+#pragma unroll
+    for (int i = 0; i < N; i++) {
+        uint32_t c = 0u;
+#pragma unroll
+        for (int j = 0; j < N; j++) {
+            const uint64_t t = (uint64_t)a[i] * b[j] + r[i + j] + c;
+            r[i + j] = (uint32_t)t;
+            c = (uint32_t)(t >> 32);
+        }
+        r[i + N] = c;
+    }
+}
+
+// bit i (compile-time) of x
+template <int I, int N>
+SFD uint32_t bit(const uint32_t (&x)[N])
+{
+    return (x[I >> 5] >> (I & 31)) & 1u;
+}
+
+// any of bits [0, K) of x, K compile-time
+template <int K, int N>
+SFD bool low_any(const uint32_t (&x)[N])
+{
+    uint32_t o = 0u;
+#pragma unroll
+    for (int i = 0; i < N; i++) {
+        if (32 * i + 32 <= K) o |= x[i];
+        else if (32 * i < K) o |= x[i] & ((1u << (K - 32 * i)) - 1u);
+    }
+    return o != 0u;
+}
+
+}  // namespace sfw

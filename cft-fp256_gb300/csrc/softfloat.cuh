@@ -1,0 +1,569 @@
+// softfloat.cuh - the element arithmetic on the GPU, one template per format.
+//
+// Semantics are the reference's (host/src/softfloat.c, with division and
+// square root as python/cft_golden/softfloat.py:440-505 defines them): five
+// rounding attributes, tininess detected after rounding, underflow only when
+// tiny AND inexact, one canonical quiet NaN, ADD/SUB/MUL as the FMA with
+// steered operands. The algorithms are this library's own:
+//
+//  * FMA: a fixed window of 2W words (W = the element's words) instead of the
+//    reference's bounded alignment. The product of the two significands,
+//    normalised to the top of the window, and the addend, aligned to it, are
+//    combined exactly wherever they overlap; bits shifted below the window
+//    are jammed into bit 0, which then acts as a sticky bit that is provably
+//    at least two places below the rounding point (see fma_general).
+//  * round_pack: normalise the window to its top bit with one variable
+//    shift, read kept/guard/sticky at fixed positions, and denormalise only
+//    for results below the normal range.
+//  * div: restoring long division to p+4 quotient bits plus a remainder
+//    sticky; sqrt: the digit-by-digit integer root to p+3 bits plus sticky.
+//    Both are exact quotient/root computations, so they round to the same
+//    bits as any other exact method.
+#pragma once
+#include "sf_words.cuh"
+
+namespace sf {
+
+// Flag bits (host/src/softfloat.h:50-55)
+constexpr uint32_t F_INVALID = 1u, F_DIVZERO = 2u, F_OVERFLOW = 4u, F_UNDERFLOW = 8u,
+                   F_INEXACT = 16u;
+// Rounding attributes (host/src/softfloat.h:57-62)
+constexpr int RNE = 0, RTZ = 1, RDN = 2, RUP = 3, RMM = 4;
+
+// Format geometry (host/src/softfloat.c:10-16). W = 32-bit words an element.
+template <int FMT> struct Fmt;
+template <> struct Fmt<0> { static constexpr int W = 1, P = 24, MANW = 23, EXPW = 8, BIAS = 127, EMAX = 127, EMIN = -126; };
+template <> struct Fmt<1> { static constexpr int W = 2, P = 53, MANW = 52, EXPW = 11, BIAS = 1023, EMAX = 1023, EMIN = -1022; };
+template <> struct Fmt<2> { static constexpr int W = 4, P = 113, MANW = 112, EXPW = 15, BIAS = 16383, EMAX = 16383, EMIN = -16382; };
+template <> struct Fmt<3> { static constexpr int W = 8, P = 237, MANW = 236, EXPW = 19, BIAS = 262143, EMAX = 262143, EMIN = -262142; };
+
+enum { C_ZERO = 0, C_SUB = 1, C_NORM = 2, C_INF = 3, C_NAN = 4 };
+
+template <int FMT>
+struct Unp {
+    static constexpr int W = Fmt<FMT>::W;
+    int cls, sign, snan;
+    int ve;             // exponent of the leading significand bit (finite non-zero)
+    uint32_t m[W];      // significand, normalised so its leading bit is bit 32W-1
+};
+
+// position of the exponent field's low bit inside the top word
+template <int FMT> __host__ __device__ constexpr int exp_shift() { return Fmt<FMT>::MANW - 32 * (Fmt<FMT>::W - 1); }
+template <int FMT> __host__ __device__ constexpr uint32_t exp_mask() { return (1u << Fmt<FMT>::EXPW) - 1u; }
+
+template <int FMT>
+SFD uint32_t exp_field(const uint32_t (&x)[Fmt<FMT>::W])
+{
+    return (x[Fmt<FMT>::W - 1] >> exp_shift<FMT>()) & exp_mask<FMT>();
+}
+
+template <int FMT>
+SFD int sign_of(const uint32_t (&x)[Fmt<FMT>::W])
+{
+    return (int)(x[Fmt<FMT>::W - 1] >> 31);
+}
+
+// Classify and unpack (host/src/softfloat.c:85-116 gives the classes).
+template <int FMT>
+SFD void unpack(const uint32_t (&x)[Fmt<FMT>::W], Unp<FMT> &u)
+{
+    using F = Fmt<FMT>;
+    constexpr int W = F::W;
+    const uint32_t ef = exp_field<FMT>(x);
+    u.sign = sign_of<FMT>(x);
+#pragma unroll
+    for (int i = 0; i < W; i++) u.m[i] = x[i];
+    u.m[W - 1] &= (1u << exp_shift<FMT>()) - 1u;          // fraction only
+    const bool fz = sfw::is_zero(u.m);
+    u.snan = 0;
+    u.ve = 0;
+    if (ef == exp_mask<FMT>()) {
+        u.cls = fz ? C_INF : C_NAN;
+        u.snan = (!fz && !((x[(F::MANW - 1) >> 5] >> ((F::MANW - 1) & 31)) & 1u)) ? 1 : 0;
+        return;
+    }
+    if (ef == 0u) {
+        if (fz) { u.cls = C_ZERO; return; }
+        u.cls = C_SUB;
+        const int L = sfw::bitlen(u.m);
+        u.ve = F::EMIN - F::MANW + L - 1;
+        sfw::shl(u.m, 32 * W - L);
+        return;
+    }
+    u.cls = C_NORM;
+    u.m[W - 1] |= 1u << exp_shift<FMT>();                  // hidden bit
+    u.ve = (int)ef - F::BIAS;
+    sfw::shl(u.m, 32 * W - F::P);
+}
+
+// ---- encodings ---------------------------------------------------------
+
+template <int FMT>
+SFD void enc_zero(uint32_t (&o)[Fmt<FMT>::W], int sign)
+{
+    sfw::zero(o);
+    o[Fmt<FMT>::W - 1] = (uint32_t)sign << 31;
+}
+
+template <int FMT>
+SFD void enc_inf(uint32_t (&o)[Fmt<FMT>::W], int sign)
+{
+    sfw::zero(o);
+    o[Fmt<FMT>::W - 1] = ((uint32_t)sign << 31) | (exp_mask<FMT>() << exp_shift<FMT>());
+}
+
+// The canonical quiet NaN: sign 0, exponent all ones, top fraction bit set
+// (host/src/softfloat.c:50-56).
+template <int FMT>
+SFD void enc_qnan(uint32_t (&o)[Fmt<FMT>::W])
+{
+    using F = Fmt<FMT>;
+    sfw::zero(o);
+    o[F::W - 1] = exp_mask<FMT>() << exp_shift<FMT>();
+    o[(F::MANW - 1) >> 5] |= 1u << ((F::MANW - 1) & 31);
+}
+
+template <int FMT>
+SFD void enc_max_normal(uint32_t (&o)[Fmt<FMT>::W], int sign)
+{
+    constexpr int W = Fmt<FMT>::W;
+#pragma unroll
+    for (int i = 0; i < W; i++) o[i] = 0xFFFFFFFFu;
+    o[W - 1] = ((uint32_t)sign << 31) | ((exp_mask<FMT>() - 1u) << exp_shift<FMT>()) |
+               ((1u << exp_shift<FMT>()) - 1u);
+}
+
+template <int FMT>
+SFD void enc_one(uint32_t (&o)[Fmt<FMT>::W], int sign)
+{
+    sfw::zero(o);
+    o[Fmt<FMT>::W - 1] = ((uint32_t)sign << 31) | ((uint32_t)Fmt<FMT>::BIAS << exp_shift<FMT>());
+}
+
+// ---- rounding (semantics: host/src/softfloat.c:120-261) ----------------
+
+SFD bool round_up(int rnd, int sign, bool guard, bool sticky, bool lsb)
+{
+    switch (rnd) {
+    case RNE: return guard && (sticky || lsb);
+    case RTZ: return false;
+    case RDN: return sign && (guard || sticky);
+    case RUP: return !sign && (guard || sticky);
+    default:  return guard;                                   // RMM
+    }
+}
+
+SFD bool overflow_to_inf(int rnd, int sign)
+{
+    return rnd == RTZ ? false : rnd == RDN ? (sign != 0) : rnd == RUP ? (sign == 0) : true;
+}
+
+// kept = the P bits of m below bit 32N (m normalised to its top bit),
+// guard = the next bit, sticky = any bit below it.
+template <int FMT, int N>
+SFD void take_top(const uint32_t (&m)[N], uint32_t (&kept)[Fmt<FMT>::W], bool &guard, bool &sticky)
+{
+    using F = Fmt<FMT>;
+    constexpr int SH = 32 * N - F::P;             // bits below the kept ones
+    static_assert(SH >= 2, "window too narrow for rounding");
+    uint32_t t[N];
+#pragma unroll
+    for (int i = 0; i < N; i++) t[i] = m[i];
+    sfw::shr_const<SH>(t);
+#pragma unroll
+    for (int i = 0; i < F::W; i++) kept[i] = t[i];
+    guard = sfw::bit<SH - 1>(m) != 0u;
+    sticky = sfw::low_any<SH - 1>(m);
+}
+
+// Round the exact non-zero value m * 2^e (m an N-word integer; its bit 0 may
+// carry a jammed sticky, which must sit at least two places below the
+// rounding point) into the format. Writes the encoding and the flags.
+template <int FMT, int N>
+SFD void round_pack(int sign, uint32_t (&m)[N], int e, int rnd, uint32_t (&out)[Fmt<FMT>::W],
+                    uint32_t &flags)
+{
+    using F = Fmt<FMT>;
+    constexpr int W = F::W;
+    const int L = sfw::bitlen(m);
+    const int e_norm = e + L - 1;                 // exponent of the leading bit
+    sfw::shl(m, 32 * N - L);                      // leading bit to the top
+
+    uint32_t kept[W];
+    bool guard, sticky;
+    take_top<FMT, N>(m, kept, guard, sticky);
+    bool up = round_up(rnd, sign, guard, sticky, kept[0] & 1u);
+
+    // Rounded as if the exponent range were unbounded: does it carry out?
+    uint32_t ones[W];
+#pragma unroll
+    for (int i = 0; i < W; i++) ones[i] = 0xFFFFFFFFu;
+    ones[W - 1] = (F::P % 32) ? ((1u << (F::P % 32)) - 1u) : 0xFFFFFFFFu;
+    const bool carry_unb = up && sfw::cmp(kept, ones) == 0;
+
+    const int d = F::EMIN - e_norm;              // > 0: below the normal range
+    if (d > 0) {
+        sfw::shr_jam(m, d);
+        take_top<FMT, N>(m, kept, guard, sticky);
+        up = round_up(rnd, sign, guard, sticky, kept[0] & 1u);
+    }
+    const bool inexact = guard || sticky;
+    uint32_t fl = inexact ? F_INEXACT : 0u;
+    if (up) sfw::inc(kept);
+
+    if (d > 0) {
+        // Subnormal (or rounded up into the smallest normal, whose bits are
+        // exactly kept's with the hidden bit landing in the exponent field).
+        const bool tiny = d >= 2 || !carry_unb;
+        if (tiny && inexact) fl |= F_UNDERFLOW;
+        if (sfw::is_zero(kept)) fl |= F_UNDERFLOW;  // rounded past the least subnormal
+#pragma unroll
+        for (int i = 0; i < W; i++) out[i] = kept[i];
+        out[W - 1] |= (uint32_t)sign << 31;
+        flags = fl;
+        return;
+    }
+    int e_res = e_norm;
+    // carry out of the top: kept == 2^P
+    static_assert(F::P < 32 * W, "kept needs room for the carry bit");
+    if (sfw::bit<F::P, W>(kept)) {
+        e_res += 1;
+        sfw::zero(kept);
+        kept[(F::P - 1) >> 5] = 1u << ((F::P - 1) & 31);
+    }
+    if (e_res > F::EMAX) {
+        if (overflow_to_inf(rnd, sign)) enc_inf<FMT>(out, sign);
+        else enc_max_normal<FMT>(out, sign);
+        flags = fl | F_OVERFLOW | F_INEXACT;
+        return;
+    }
+#pragma unroll
+    for (int i = 0; i < W; i++) out[i] = kept[i];
+    out[W - 1] &= (1u << exp_shift<FMT>()) - 1u;   // drop the hidden bit
+    out[W - 1] |= ((uint32_t)sign << 31) | ((uint32_t)(e_res + F::BIAS) << exp_shift<FMT>());
+    flags = fl;
+}
+
+// ---- fused multiply-add ---------------------------------------------------
+
+template <int FMT>
+SFD bool any_snan(const Unp<FMT> &a, const Unp<FMT> &b, const Unp<FMT> &c)
+{
+    return (a.cls == C_NAN && a.snan) || (b.cls == C_NAN && b.snan) || (c.cls == C_NAN && c.snan);
+}
+
+// The steered operand kinds: FMA a*b+c; ADD a*1+c; SUB a*1+(-c); MUL a*b+(+-0)
+// (host/src/softfloat.c:438-468).
+enum { OP_FMA = 0, OP_ADD = 1, OP_SUB = 2, OP_MUL = 3 };
+
+// The general path: finite non-zero a and b; c finite (zero allowed).
+//
+// Window: N = 2W words. a's significand is placed with its leading bit at
+// 32W-2 and b's at 32W-1, so their product's leading bit is at 64W-3 or
+// 64W-2 and bit 64W-1 is free for a carry. Its low 64W-2P-1 bits are zero.
+// The addend's leading bit is aligned to 64W-2, its low 64W-P-1 bits zero.
+// With delta = (addend exponent) - (product's nominal exponent) - 1:
+//  * delta > 0: the product is shifted right by delta. Exact for delta <= 1
+//    (the only shifts after which the two can cancel to fewer than P+2
+//    bits); for delta >= 2 the difference keeps its leading bit at 64W-3 or
+//    above, so a jammed bit 0 is far below the rounding point.
+//  * delta < 0: the addend is shifted right by -delta; bits are lost only
+//    when its leading bit falls below bit P, where it cannot cancel the
+//    product's leading bits.
+// A jammed bit 0 makes the computed window W' satisfy: bits >= 1 of W' are
+// floor(exact/2) and bit 0 is set iff the exact value is not an integer
+// (operands' true low bits are zero there, so subtracting a jammed operand
+// leaves bit 0 set). Rounding at any position >= 2 then reads the right
+// kept bits, guard and sticky.
+template <int FMT, int OP>
+SFD void fma_general(const Unp<FMT> &ua, const Unp<FMT> &ub, const Unp<FMT> &uc, int sc, int rnd,
+                     uint32_t (&out)[Fmt<FMT>::W], uint32_t &flags)
+{
+    using F = Fmt<FMT>;
+    constexpr int W = F::W, N = 2 * W;
+    uint32_t P[N];
+    const int sp = ua.sign ^ ub.sign;
+    int ew;                                        // weight of window bit 0
+    if constexpr (OP == OP_ADD || OP == OP_SUB) {
+        // a * 1.0 needs no multiply: the product is a's significand placed
+        // where the multiply would have put it, leading bit at 64W-3.
+#pragma unroll
+        for (int i = 0; i < W; i++) P[i] = 0u;
+#pragma unroll
+        for (int i = 0; i < W; i++) P[W + i] = ua.m[i];   // leading bit at 64W-1
+        sfw::shr_const<2>(P);                              // leading bit at 64W-3
+        ew = ua.ve - (64 * W - 3);
+    } else {
+        uint32_t ma[W];
+#pragma unroll
+        for (int i = 0; i < W; i++) ma[i] = ua.m[i];
+        sfw::shr_const<1>(ma);                     // leading bit at 32W-2
+        sfw::mul<W>(P, ma, ub.m);
+        ew = ua.ve + ub.ve - (64 * W - 3);
+    }
+
+    int rs = sp;
+    if (uc.cls != C_ZERO) {
+        uint32_t C[N];
+#pragma unroll
+        for (int i = 0; i < W; i++) C[i] = 0u;
+#pragma unroll
+        for (int i = 0; i < W; i++) C[W + i] = uc.m[i];
+        sfw::shr_const<1>(C);                      // leading bit at 64W-2
+        const int delta = uc.ve - (ew + 64 * W - 2);
+        if (delta > 0) {
+            sfw::shr_jam(P, delta);
+            ew += delta;
+        } else if (delta < 0) {
+            sfw::shr_jam(C, -delta);
+        }
+        if (sp == sc) {
+            sfw::add(P, P, C);
+        } else {
+            const uint32_t br = sfw::sub(P, P, C);
+            if (br) {
+                sfw::neg(P);
+                rs = sc;
+            }
+            if (sfw::is_zero(P)) {                 // exact cancellation
+                enc_zero<FMT>(out, rnd == RDN ? 1 : 0);
+                flags = 0u;
+                return;
+            }
+        }
+    }
+    round_pack<FMT, N>(rs, P, ew, rnd, out, flags);
+}
+
+// One element of FMA/ADD/SUB/MUL. x/y/z are the caller's a, b, c (b unused
+// for ADD/SUB, c unused for MUL). Special cases follow the reference's
+// order (host/src/softfloat.c:335-373).
+template <int FMT, int OP>
+SFD void arith(const uint32_t (&x)[Fmt<FMT>::W], const uint32_t (&y)[Fmt<FMT>::W],
+               const uint32_t (&z)[Fmt<FMT>::W], int rnd, uint32_t (&out)[Fmt<FMT>::W],
+               uint32_t &flags)
+{
+    using F = Fmt<FMT>;
+    constexpr int W = F::W;
+    Unp<FMT> ua, ub, uc;
+    uint32_t bsteer[W], csteer[W];
+    // steering
+    if constexpr (OP == OP_ADD || OP == OP_SUB) {
+        enc_one<FMT>(bsteer, 0);
+    } else {
+#pragma unroll
+        for (int i = 0; i < W; i++) bsteer[i] = y[i];
+    }
+    if constexpr (OP == OP_MUL) {
+        enc_zero<FMT>(csteer, sign_of<FMT>(x) ^ sign_of<FMT>(y));
+    } else {
+#pragma unroll
+        for (int i = 0; i < W; i++) csteer[i] = z[i];
+        if constexpr (OP == OP_SUB) csteer[W - 1] ^= 0x80000000u;
+    }
+    unpack<FMT>(x, ua);
+    unpack<FMT>(bsteer, ub);
+    unpack<FMT>(csteer, uc);
+    flags = 0u;
+
+    if (ua.cls == C_NAN || ub.cls == C_NAN || uc.cls == C_NAN) {
+        enc_qnan<FMT>(out);
+        flags = any_snan(ua, ub, uc) ? F_INVALID : 0u;
+        return;
+    }
+    const int sp = ua.sign ^ ub.sign;
+    if (ua.cls == C_INF || ub.cls == C_INF) {
+        if (ua.cls == C_ZERO || ub.cls == C_ZERO || (uc.cls == C_INF && uc.sign != sp)) {
+            enc_qnan<FMT>(out);                    // inf * 0, inf - inf
+            flags = F_INVALID;
+            return;
+        }
+        enc_inf<FMT>(out, sp);
+        return;
+    }
+    if (uc.cls == C_INF) {
+        enc_inf<FMT>(out, uc.sign);
+        return;
+    }
+    if (ua.cls == C_ZERO || ub.cls == C_ZERO) {
+        if (uc.cls == C_ZERO) {
+            enc_zero<FMT>(out, uc.sign == sp ? uc.sign : (rnd == RDN ? 1 : 0));
+            return;
+        }
+#pragma unroll
+        for (int i = 0; i < W; i++) out[i] = csteer[i];   // 0*b + c is c, exactly
+        return;
+    }
+    fma_general<FMT, OP>(ua, ub, uc, uc.sign, rnd, out, flags);
+}
+
+// ---- division (definition: python/cft_golden/softfloat.py:440-471) ------
+
+template <int FMT>
+SFD void div(const uint32_t (&x)[Fmt<FMT>::W], const uint32_t (&y)[Fmt<FMT>::W], int rnd,
+             uint32_t (&out)[Fmt<FMT>::W], uint32_t &flags)
+{
+    using F = Fmt<FMT>;
+    constexpr int W = F::W;
+    Unp<FMT> ua, ub;
+    unpack<FMT>(x, ua);
+    unpack<FMT>(y, ub);
+    flags = 0u;
+    if (ua.cls == C_NAN || ub.cls == C_NAN) {
+        enc_qnan<FMT>(out);
+        flags = ((ua.cls == C_NAN && ua.snan) || (ub.cls == C_NAN && ub.snan)) ? F_INVALID : 0u;
+        return;
+    }
+    const int sq = ua.sign ^ ub.sign;
+    if (ua.cls == C_INF) {
+        if (ub.cls == C_INF) { enc_qnan<FMT>(out); flags = F_INVALID; return; }
+        enc_inf<FMT>(out, sq);
+        return;
+    }
+    if (ub.cls == C_INF) { enc_zero<FMT>(out, sq); return; }
+    if (ub.cls == C_ZERO) {
+        if (ua.cls == C_ZERO) { enc_qnan<FMT>(out); flags = F_INVALID; return; }
+        enc_inf<FMT>(out, sq);
+        flags = F_DIVZERO;
+        return;
+    }
+    if (ua.cls == C_ZERO) { enc_zero<FMT>(out, sq); return; }
+
+    // Both significands have their leading bit at 32W-1. Restoring division
+    // of X by Y produces Q = P+4 quotient bits; the first may be zero, so at
+    // least P+3 are significant. The remainder r < Y always, and r << 1 may
+    // need bit 32W: kept in `top`.
+    constexpr int Q = F::P + 4;
+    constexpr int NQ = (Q + 1 + 31) / 32;          // quotient + sticky bit
+    uint32_t r[W], q[NQ];
+#pragma unroll
+    for (int i = 0; i < W; i++) r[i] = ua.m[i];
+    sfw::zero(q);
+    uint32_t top = 0u;
+#pragma unroll 1
+    for (int k = 0; k < Q; k++) {
+        uint32_t t[W];
+        const uint32_t br = sfw::sub(t, r, ub.m);
+        const bool ge = top || !br;
+        if (ge) {
+#pragma unroll
+            for (int i = 0; i < W; i++) r[i] = t[i];
+        }
+        // q = (q << 1) | ge
+#pragma unroll
+        for (int i = NQ - 1; i >= 1; i--) q[i] = __funnelshift_l(q[i - 1], q[i], 1);
+        q[0] = (q[0] << 1) | (ge ? 1u : 0u);
+        // r <<= 1 (skipped after the last digit)
+        top = r[W - 1] >> 31;
+#pragma unroll
+        for (int i = W - 1; i >= 1; i--) r[i] = __funnelshift_l(r[i - 1], r[i], 1);
+        r[0] <<= 1;
+    }
+    // After the loop r holds 2*rem (and top its overflow); any non-zero is sticky.
+    const bool rem = top || !sfw::is_zero(r);
+#pragma unroll
+    for (int i = NQ - 1; i >= 1; i--) q[i] = __funnelshift_l(q[i - 1], q[i], 1);
+    q[0] = (q[0] << 1) | (rem ? 1u : 0u);
+    // value = q * 2^e: the first quotient bit has weight 2^(ve_a - ve_b)
+    const int e = ua.ve - ub.ve - Q;
+    round_pack<FMT, NQ>(sq, q, e, rnd, out, flags);
+}
+
+// ---- square root (definition: python/cft_golden/softfloat.py:474-505) ---
+
+template <int FMT>
+SFD void sqrt(const uint32_t (&x)[Fmt<FMT>::W], int rnd, uint32_t (&out)[Fmt<FMT>::W],
+              uint32_t &flags)
+{
+    using F = Fmt<FMT>;
+    constexpr int W = F::W;
+    Unp<FMT> ua;
+    unpack<FMT>(x, ua);
+    flags = 0u;
+    if (ua.cls == C_NAN) {
+        enc_qnan<FMT>(out);
+        flags = ua.snan ? F_INVALID : 0u;
+        return;
+    }
+    if (ua.cls == C_ZERO) {
+#pragma unroll
+        for (int i = 0; i < W; i++) out[i] = x[i];
+        return;
+    }
+    if (ua.sign) { enc_qnan<FMT>(out); flags = F_INVALID; return; }
+    if (ua.cls == C_INF) {
+#pragma unroll
+        for (int i = 0; i < W; i++) out[i] = x[i];
+        return;
+    }
+    // Radicand: the significand (leading bit at 32W-1, value m * 2^(ve-32W+1))
+    // shifted so its exponent is even and the root has R = P+3 bits. Let the
+    // radicand X = m_top * 2^(k) as a 2R-bit integer with X in [2^(2R-2), 2^(2R)).
+    constexpr int R = F::P + 3;
+    constexpr int NX = (2 * R + 31) / 32;           // radicand words
+    constexpr int NR = (R + 1 + 31) / 32;           // root + sticky
+    // exponent of the radicand's bit 0 must be even; place m's leading bit at
+    // bit 2R-1 or 2R-2 accordingly.
+    uint32_t X[NX];
+    sfw::zero(X);
+    // leading bit position in X: 2R-1 if (ve - (2R-1)) is even, else 2R-2
+    const int lead = ((ua.ve - (2 * R - 1)) & 1) ? (2 * R - 2) : (2 * R - 1);
+    const int ex = ua.ve - lead;                     // even
+    {
+        // place ua.m (leading bit 32W-1) so its leading bit is at `lead`
+        uint32_t t[NX];
+        sfw::zero(t);
+        constexpr int OFF = NX - W;                 // put m in the top W words
+#pragma unroll
+        for (int i = 0; i < W; i++) t[OFF + i] = ua.m[i];
+        // leading bit is now at 32NX-1; shift right to `lead` (no bits lost:
+        // the significand has P <= 2R - 32(NX - W) ... enough low zeros)
+        sfw::shr_jam(t, 32 * NX - 1 - lead);
+#pragma unroll
+        for (int i = 0; i < NX; i++) X[i] = t[i];
+    }
+    // digit-by-digit root: R iterations over bit pairs from the top
+    uint32_t rem[NX], res[NX];
+    sfw::zero(rem);
+    sfw::zero(res);
+#pragma unroll 1
+    for (int k = R - 1; k >= 0; k--) {
+        // rem = (rem << 2) | X[2k+1:2k]
+        const int bp = 2 * k;
+        uint32_t two = 0u;
+#pragma unroll
+        for (int i = 0; i < NX; i++)
+            if (i == (bp >> 5)) two = (X[i] >> (bp & 31)) & 3u;
+#pragma unroll
+        for (int i = NX - 1; i >= 1; i--) rem[i] = __funnelshift_l(rem[i - 1], rem[i], 2);
+        rem[0] = (rem[0] << 2) | two;
+        // trial = (res << 2) | 1
+        uint32_t tr[NX];
+#pragma unroll
+        for (int i = NX - 1; i >= 1; i--) tr[i] = __funnelshift_l(res[i - 1], res[i], 2);
+        tr[0] = (res[0] << 2) | 1u;
+        uint32_t d[NX];
+        const uint32_t br = sfw::sub(d, rem, tr);
+#pragma unroll
+        for (int i = NX - 1; i >= 1; i--) res[i] = __funnelshift_l(res[i - 1], res[i], 1);
+        res[0] <<= 1;
+        if (!br) {
+#pragma unroll
+            for (int i = 0; i < NX; i++) rem[i] = d[i];
+            res[0] |= 1u;
+        }
+    }
+    // res has R bits (leading bit set since X >= 2^(2R-2)); fold sticky
+    uint32_t m[NR];
+#pragma unroll
+    for (int i = 0; i < NR; i++) m[i] = 0u;
+#pragma unroll
+    for (int i = 0; i < NR && i < NX; i++) m[i] = res[i];
+#pragma unroll
+    for (int i = NR - 1; i >= 1; i--) m[i] = __funnelshift_l(m[i - 1], m[i], 1);
+    m[0] = (m[0] << 1) | (sfw::is_zero(rem) ? 0u : 1u);
+    // root value = res * 2^(ex/2); m = 2*res + sticky -> exponent ex/2 - 1
+    round_pack<FMT, NR>(0, m, (ex >> 1) - 1, rnd, out, flags);
+}
+
+}  // namespace sf

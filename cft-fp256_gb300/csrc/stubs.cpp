@@ -1,0 +1,105 @@
+// stubs.cpp - the reference entry points outside this backend's scope
+// (include/cft_unsupported.h). Each refuses by name so that a binding
+// written for the reference loads and a call outside the hot path says why
+// it cannot run here, instead of computing on the CPU.
+#include "../../include/cft_unsupported.h"
+#include "api_core.h"
+
+using cftg::clear_error;
+using cftg::set_error;
+
+static cft_status refuse(const char *who)
+{
+    set_error("%s: this GB300 backend carries the elementwise arithmetic path (cft_run, cft_run_ex, "
+              "cft_div, cft_sqrt) and the sequencer; %s is outside it",
+              who, who);
+    return CFT_ERR_UNSUPPORTED;
+}
+
+extern "C" cft_status cft_exp(cft_device *, cft_format, cft_round, const void *, void *, size_t, uint32_t *) { clear_error(); return refuse("cft_exp"); }
+extern "C" cft_status cft_expm1(cft_device *, cft_format, cft_round, const void *, void *, size_t, uint32_t *) { clear_error(); return refuse("cft_expm1"); }
+extern "C" cft_status cft_exp2(cft_device *, cft_format, cft_round, const void *, void *, size_t, uint32_t *) { clear_error(); return refuse("cft_exp2"); }
+extern "C" cft_status cft_log(cft_device *, cft_format, cft_round, const void *, void *, size_t, uint32_t *) { clear_error(); return refuse("cft_log"); }
+extern "C" cft_status cft_log1p(cft_device *, cft_format, cft_round, const void *, void *, size_t, uint32_t *) { clear_error(); return refuse("cft_log1p"); }
+extern "C" cft_status cft_log2(cft_device *, cft_format, cft_round, const void *, void *, size_t, uint32_t *) { clear_error(); return refuse("cft_log2"); }
+extern "C" cft_status cft_log10(cft_device *, cft_format, cft_round, const void *, void *, size_t, uint32_t *) { clear_error(); return refuse("cft_log10"); }
+extern "C" cft_status cft_sinpi(cft_device *, cft_format, cft_round, const void *, void *, size_t, uint32_t *) { clear_error(); return refuse("cft_sinpi"); }
+extern "C" cft_status cft_cospi(cft_device *, cft_format, cft_round, const void *, void *, size_t, uint32_t *) { clear_error(); return refuse("cft_cospi"); }
+extern "C" cft_status cft_tanpi(cft_device *, cft_format, cft_round, const void *, void *, size_t, uint32_t *) { clear_error(); return refuse("cft_tanpi"); }
+extern "C" cft_status cft_asin(cft_device *, cft_format, cft_round, const void *, void *, size_t, uint32_t *) { clear_error(); return refuse("cft_asin"); }
+extern "C" cft_status cft_acos(cft_device *, cft_format, cft_round, const void *, void *, size_t, uint32_t *) { clear_error(); return refuse("cft_acos"); }
+extern "C" cft_status cft_atan(cft_device *, cft_format, cft_round, const void *, void *, size_t, uint32_t *) { clear_error(); return refuse("cft_atan"); }
+extern "C" cft_status cft_asinpi(cft_device *, cft_format, cft_round, const void *, void *, size_t, uint32_t *) { clear_error(); return refuse("cft_asinpi"); }
+extern "C" cft_status cft_acospi(cft_device *, cft_format, cft_round, const void *, void *, size_t, uint32_t *) { clear_error(); return refuse("cft_acospi"); }
+extern "C" cft_status cft_atanpi(cft_device *, cft_format, cft_round, const void *, void *, size_t, uint32_t *) { clear_error(); return refuse("cft_atanpi"); }
+extern "C" cft_status cft_sin(cft_device *, cft_format, cft_round, const void *, void *, size_t, uint32_t *) { clear_error(); return refuse("cft_sin"); }
+extern "C" cft_status cft_cos(cft_device *, cft_format, cft_round, const void *, void *, size_t, uint32_t *) { clear_error(); return refuse("cft_cos"); }
+extern "C" cft_status cft_tan(cft_device *, cft_format, cft_round, const void *, void *, size_t, uint32_t *) { clear_error(); return refuse("cft_tan"); }
+extern "C" cft_status cft_sinh(cft_device *, cft_format, cft_round, const void *, void *, size_t, uint32_t *) { clear_error(); return refuse("cft_sinh"); }
+extern "C" cft_status cft_cosh(cft_device *, cft_format, cft_round, const void *, void *, size_t, uint32_t *) { clear_error(); return refuse("cft_cosh"); }
+extern "C" cft_status cft_tanh(cft_device *, cft_format, cft_round, const void *, void *, size_t, uint32_t *) { clear_error(); return refuse("cft_tanh"); }
+extern "C" cft_status cft_asinh(cft_device *, cft_format, cft_round, const void *, void *, size_t, uint32_t *) { clear_error(); return refuse("cft_asinh"); }
+extern "C" cft_status cft_acosh(cft_device *, cft_format, cft_round, const void *, void *, size_t, uint32_t *) { clear_error(); return refuse("cft_acosh"); }
+extern "C" cft_status cft_atanh(cft_device *, cft_format, cft_round, const void *, void *, size_t, uint32_t *) { clear_error(); return refuse("cft_atanh"); }
+extern "C" cft_status cft_exp2m1(cft_device *, cft_format, cft_round, const void *, void *, size_t, uint32_t *) { clear_error(); return refuse("cft_exp2m1"); }
+extern "C" cft_status cft_exp10(cft_device *, cft_format, cft_round, const void *, void *, size_t, uint32_t *) { clear_error(); return refuse("cft_exp10"); }
+extern "C" cft_status cft_exp10m1(cft_device *, cft_format, cft_round, const void *, void *, size_t, uint32_t *) { clear_error(); return refuse("cft_exp10m1"); }
+extern "C" cft_status cft_log2p1(cft_device *, cft_format, cft_round, const void *, void *, size_t, uint32_t *) { clear_error(); return refuse("cft_log2p1"); }
+extern "C" cft_status cft_log10p1(cft_device *, cft_format, cft_round, const void *, void *, size_t, uint32_t *) { clear_error(); return refuse("cft_log10p1"); }
+extern "C" cft_status cft_rsqrt(cft_device *, cft_format, cft_round, const void *, void *, size_t, uint32_t *) { clear_error(); return refuse("cft_rsqrt"); }
+extern "C" cft_status cft_pow(cft_device *, cft_format, cft_round, const void *, const void *, void *, size_t, uint32_t *) { clear_error(); return refuse("cft_pow"); }
+extern "C" cft_status cft_hypot(cft_device *, cft_format, cft_round, const void *, const void *, void *, size_t, uint32_t *) { clear_error(); return refuse("cft_hypot"); }
+extern "C" cft_status cft_atan2(cft_device *, cft_format, cft_round, const void *, const void *, void *, size_t, uint32_t *) { clear_error(); return refuse("cft_atan2"); }
+extern "C" cft_status cft_atan2pi(cft_device *, cft_format, cft_round, const void *, const void *, void *, size_t, uint32_t *) { clear_error(); return refuse("cft_atan2pi"); }
+extern "C" cft_status cft_powr(cft_device *, cft_format, cft_round, const void *, const void *, void *, size_t, uint32_t *) { clear_error(); return refuse("cft_powr"); }
+extern "C" cft_status cft_pown(cft_device *, cft_format, cft_round, const void *, const int64_t *, void *, size_t, uint32_t *) { clear_error(); return refuse("cft_pown"); }
+extern "C" cft_status cft_compound(cft_device *, cft_format, cft_round, const void *, const int64_t *, void *, size_t, uint32_t *) { clear_error(); return refuse("cft_compound"); }
+extern "C" cft_status cft_rootn(cft_device *, cft_format, cft_round, const void *, const int64_t *, void *, size_t, uint32_t *) { clear_error(); return refuse("cft_rootn"); }
+extern "C" cft_status cft_augmented_add(cft_device *, cft_format, const void *, const void *, void *, void *, size_t, uint32_t *) { clear_error(); return refuse("cft_augmented_add"); }
+extern "C" cft_status cft_augmented_sub(cft_device *, cft_format, const void *, const void *, void *, void *, size_t, uint32_t *) { clear_error(); return refuse("cft_augmented_sub"); }
+extern "C" cft_status cft_augmented_mul(cft_device *, cft_format, const void *, const void *, void *, void *, size_t, uint32_t *) { clear_error(); return refuse("cft_augmented_mul"); }
+extern "C" cft_status cft_scaled_prod(cft_device *, cft_format, cft_round, const void *, void *, int64_t *, size_t, uint32_t *) { clear_error(); return refuse("cft_scaled_prod"); }
+extern "C" cft_status cft_scaled_prod_sum(cft_device *, cft_format, cft_round, const void *, const void *, void *, int64_t *, size_t, uint32_t *) { clear_error(); return refuse("cft_scaled_prod_sum"); }
+extern "C" cft_status cft_scaled_prod_diff(cft_device *, cft_format, cft_round, const void *, const void *, void *, int64_t *, size_t, uint32_t *) { clear_error(); return refuse("cft_scaled_prod_diff"); }
+extern "C" cft_status cft_formatof_add(cft_device *, cft_format, cft_format, cft_round, const void *, const void *, void *, size_t, uint32_t *, uint32_t *) { clear_error(); return refuse("cft_formatof_add"); }
+extern "C" cft_status cft_formatof_sub(cft_device *, cft_format, cft_format, cft_round, const void *, const void *, void *, size_t, uint32_t *, uint32_t *) { clear_error(); return refuse("cft_formatof_sub"); }
+extern "C" cft_status cft_formatof_mul(cft_device *, cft_format, cft_format, cft_round, const void *, const void *, void *, size_t, uint32_t *, uint32_t *) { clear_error(); return refuse("cft_formatof_mul"); }
+extern "C" cft_status cft_formatof_div(cft_device *, cft_format, cft_format, cft_round, const void *, const void *, void *, size_t, uint32_t *, uint32_t *) { clear_error(); return refuse("cft_formatof_div"); }
+extern "C" cft_status cft_formatof_sqrt(cft_device *, cft_format, cft_format, cft_round, const void *, void *, size_t, uint32_t *, uint32_t *) { clear_error(); return refuse("cft_formatof_sqrt"); }
+extern "C" cft_status cft_formatof_fma(cft_device *, cft_format, cft_format, cft_round, const void *, const void *, const void *, void *, size_t, uint32_t *, uint32_t *) { clear_error(); return refuse("cft_formatof_fma"); }
+// decimal digits a format needs to round-trip (754-2019 5.12.2: 1 + ceil(p log10 2)); a pure
+// function of the format, so it is answered rather than refused
+extern "C" size_t cft_format_decimal_digits(cft_format fmt)
+{
+    static const size_t d[4] = {9, 17, 36, 73};
+    return ((int)fmt >= 0 && (int)fmt <= 3) ? d[(int)fmt] : 0;
+}
+extern "C" cft_status cft_from_decimal_char(cft_device *, cft_format, cft_round, const char *const *, void *, size_t, size_t *, uint32_t *) { clear_error(); return refuse("cft_from_decimal_char"); }
+extern "C" cft_status cft_from_hex_char(cft_device *, cft_format, cft_round, const char *const *, void *, size_t, size_t *, uint32_t *) { clear_error(); return refuse("cft_from_hex_char"); }
+extern "C" cft_status cft_to_decimal_char(cft_device *, cft_format, cft_round, const void *, size_t, char *, size_t, size_t *, uint32_t *) { clear_error(); return refuse("cft_to_decimal_char"); }
+extern "C" cft_status cft_to_hex_char(cft_device *, cft_format, const void *, char *, size_t, size_t *) { clear_error(); return refuse("cft_to_hex_char"); }
+extern "C" cft_status cft_get_payload(cft_device *, cft_format, const void *, void *, size_t) { clear_error(); return refuse("cft_get_payload"); }
+extern "C" cft_status cft_set_payload(cft_device *, cft_format, const void *, void *, size_t) { clear_error(); return refuse("cft_set_payload"); }
+extern "C" cft_status cft_set_payload_signaling(cft_device *, cft_format, const void *, void *, size_t) { clear_error(); return refuse("cft_set_payload_signaling"); }
+extern "C" cft_status cft_min_mag(cft_device *, cft_format, const void *, const void *, void *, size_t, uint32_t *) { clear_error(); return refuse("cft_min_mag"); }
+extern "C" cft_status cft_max_mag(cft_device *, cft_format, const void *, const void *, void *, size_t, uint32_t *) { clear_error(); return refuse("cft_max_mag"); }
+extern "C" cft_status cft_minnum_mag(cft_device *, cft_format, const void *, const void *, void *, size_t, uint32_t *) { clear_error(); return refuse("cft_minnum_mag"); }
+extern "C" cft_status cft_maxnum_mag(cft_device *, cft_format, const void *, const void *, void *, size_t, uint32_t *) { clear_error(); return refuse("cft_maxnum_mag"); }
+
+// reductions: "next" for this backend (cft_supports answers 0 for them)
+extern "C" cft_status cft_reduce(cft_device *dev, cft_op, cft_format, cft_round, const void *, const void *,
+                                 void *, size_t, uint32_t *, uint32_t *bus_out)
+{
+    clear_error();
+    if (bus_out) *bus_out = 0;
+    if (!dev) return CFT_ERR_INVALID_ARGUMENT;
+    return refuse("cft_reduce");
+}
+extern "C" cft_status cft_reduce_seg(cft_device *dev, cft_op, cft_format, cft_round, const void *,
+                                     const void *, void *, size_t, size_t, uint32_t *, uint32_t *bus_out)
+{
+    clear_error();
+    if (bus_out) *bus_out = 0;
+    if (!dev) return CFT_ERR_INVALID_ARGUMENT;
+    return refuse("cft_reduce_seg");
+}

@@ -1,0 +1,47 @@
+/* cft_gb300.h - entry points this library adds beside the reference's C ABI
+ * (include/cft.h). None replaces a reference call; each exists so that a
+ * caller holding DEVICE memory (a PyTorch CUDA tensor, a buffer another
+ * CUDA library produced) can run the same arithmetic without a host round
+ * trip, and so the batched and serving forms have a C surface.
+ *
+ * Semantics are exactly cft_run's / cft_div's / cft_sqrt's for the same
+ * element values: same bits, same flags. Pointers are device pointers;
+ * elements are the same dense little-endian byte strings.
+ */
+#ifndef CFT_GB300_H
+#define CFT_GB300_H
+
+#include "cft.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Work kinds for the device-pointer calls. */
+#define CFTG_KIND_OP   0   /* opcode `op`, as cft_run */
+#define CFTG_KIND_DIV  1   /* a / b, as cft_div */
+#define CFTG_KIND_SQRT 2   /* sqrt(a), as cft_sqrt */
+
+/* One elementwise launch over device memory, asynchronous on `stream`
+ * (a cudaStream_t; NULL is the legacy default stream). The call's flags
+ * are ORed into the device word *flags_word (the caller zeroes it and
+ * reads it back); lane_flags, when non-NULL, receives each element's flag
+ * byte. A NULL b or c reads +0. scalar_mask bit r makes operand r element
+ * 0 for every i. The status word of the handle is NOT updated: the flags
+ * stay on the device until the caller reads them. */
+CFT_API cft_status cftg_run_device(cft_device *dev, int kind, cft_op op, cft_format fmt,
+                                   cft_round rnd, const void *a, const void *b, const void *c,
+                                   void *d, size_t n, uint32_t scalar_mask, uint8_t *lane_flags,
+                                   uint32_t *flags_word, void *stream);
+
+/* The CUDA device ordinal a handle runs on. */
+CFT_API int cftg_device_ordinal(cft_device *dev);
+
+/* The sequencer features this build publishes in cft_caps.seq_features. */
+CFT_API uint32_t cftg_seq_features(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CFT_GB300_H */
