@@ -49,6 +49,7 @@ struct SeqProgram {
     uint32_t scratch_used = 0, scratch_depth = 256, scratch_log2 = 8;
     int scratch_active = 0;
     uint32_t reach = 0;                       // slots a lane's scratch clears
+    uint32_t nregs = 32;                      // registers the program names (highest + 1)
     const uint64_t *d_insns = nullptr;        // device copy of the instruction words
     const void *d_consts = nullptr;           // device constants (or the run's bank)
     const int32_t *d_endrep = nullptr;        // REPEAT pc -> matching ENDREP pc

@@ -1,0 +1,399 @@
+// seq.cu - the sequencer on the GPU: one thread a lane, a warp a block of
+// lanes, every control decision taken per warp.
+//
+// The program model is the reference's (host/src/seq_exec.h:412-923). Its
+// executor runs lanes in blocks and lets REPEAT/ENDREP skip a loop only
+// when no lane of the block is active; the reference argues that the
+// block size is invisible in the results (host/src/program.c:11-31): an
+// inactive lane writes, deposits and raises nothing, and ACTALL and HALT
+// are refused inside loops. Here the block is the warp. Control flow is
+// therefore warp-uniform (decided with __any_sync), every lane of a warp
+// decodes the same instruction from a broadcast load, and only the
+// arithmetic itself - one element of the opcode per active lane - runs
+// per thread.
+//
+// A lane's 32 registers live in shared memory, structure-of-words
+// (word w of register r of lane t at [(r*W + w)*T + t]), so a warp's
+// accesses to one register hit 32 consecutive banks. Only the registers
+// the program names are allocated. Scratch slots live in global memory in
+// the same structure-of-words layout across the launch's lanes.
+#include "cftg_internal.h"
+#include "simple_ops.cuh"
+
+namespace cftg {
+
+namespace {
+
+constexpr uint32_t NONE = 0xFFFFFFFFu;
+
+struct Insn {
+    int op, rd, ra, rb, rc, rnd, ka, kb, kc, kx, ctrl;
+    uint32_t imm;
+};
+
+// instruction word fields (reference seq_exec.h:175-200)
+SFD Insn decode(uint64_t w)
+{
+    Insn d;
+    d.op = (int)(w & 0xFF);
+    d.rd = (int)((w >> 8) & 0xF);
+    d.ra = (int)((w >> 12) & 0xF);
+    d.rb = (int)((w >> 16) & 0xF);
+    d.rc = (int)((w >> 20) & 0xF);
+    d.rnd = (int)((w >> 24) & 0x7);
+    d.ka = (int)((w >> 27) & 1);
+    d.kb = (int)((w >> 28) & 1);
+    d.kc = (int)((w >> 29) & 1);
+    d.kx = (int)((w >> 30) & 1);
+    d.ctrl = (int)((w >> 31) & 1);
+    d.imm = (uint32_t)(w >> 32);
+    return d;
+}
+
+SFD int reg5(int lo, uint32_t imm, int which) { return lo | (int)(((imm >> (24 + which)) & 1u) << 4); }
+
+// operand `which` (0 a, 1 b, 2 c): register number or constant index
+// (reference seq_exec.h:232-246)
+SFD int source(const Insn &d, int which, bool &is_const)
+{
+    const int kf = which == 0 ? d.ka : which == 1 ? d.kb : d.kc;
+    const int reg = which == 0 ? d.ra : which == 1 ? d.rb : d.rc;
+    is_const = kf != 0;
+    if (!kf) return reg5(reg, d.imm, 1 + which);
+    if (d.kx) return (int)((d.imm >> (8 * which)) & 0xFFu) | (int)(((d.imm >> (28 + which)) & 1u) << 8);
+    return reg;
+}
+
+template <int W>
+struct Lane {
+    uint32_t *sm;       // this block's register file
+    int T, t;           // lanes in the block, this lane's index
+    SFD uint32_t &at(int r, int w) const { return sm[(r * W + w) * T + t]; }
+    SFD void get(int r, uint32_t (&x)[W]) const
+    {
+#pragma unroll
+        for (int w = 0; w < W; w++) x[w] = at(r, w);
+    }
+    SFD void put(int r, const uint32_t (&x)[W]) const
+    {
+#pragma unroll
+        for (int w = 0; w < W; w++) at(r, w) = x[w];
+    }
+};
+
+template <int W>
+SFD void load_elem_g(const void *base, size_t j, uint32_t (&x)[W])
+{
+    const uint32_t *p = static_cast<const uint32_t *>(base) + j * W;
+#pragma unroll
+    for (int w = 0; w < W; w++) x[w] = p[w];
+}
+
+template <int W>
+SFD void load_in(const void *src, const uint32_t *idx, size_t e, uint32_t (&x)[W])
+{
+    if (idx) {
+        const uint32_t t = idx[e];
+        if (t == NONE) {
+            sfw::zero(x);
+            return;
+        }
+        load_elem_g<W>(src, t, x);
+        return;
+    }
+    load_elem_g<W>(src, e, x);
+}
+
+}  // namespace
+
+template <int FMT>
+__global__ void k_seq(const SeqLaunch L, size_t lane0, size_t nl)
+{
+    constexpr int W = sf::Fmt<FMT>::W;
+    extern __shared__ uint32_t smem[];
+    const SeqProgram &P = L.P;
+    const int T = blockDim.x, t = threadIdx.x;
+    const size_t local = (size_t)blockIdx.x * T + t;
+    const size_t lane = lane0 + local;
+    const bool have = local < nl;
+    const int nregs = (int)P.nregs;
+    const uint32_t log2d = P.scratch_log2;
+    Lane<W> R{smem, T, t};
+
+    bool keep = have;
+    if (have && L.lane_mask) keep = (L.lane_mask[lane >> 3] >> (lane & 7)) & 1u;
+    bool active = keep;
+
+    // registers +0, then r0..r2 from the streams (reference seq_exec.h:810-860)
+    for (int r = 0; r < nregs; r++) {
+#pragma unroll
+        for (int w = 0; w < W; w++) R.at(r, w) = 0u;
+    }
+    uint32_t x[W];
+    if (keep) {
+        if (nregs > 0) { load_in<W>(L.a, L.ia, lane, x); R.put(0, x); }
+        if (nregs > 1 && L.b) { load_in<W>(L.b, L.ib, lane, x); R.put(1, x); }
+        if (nregs > 2 && L.c) { load_in<W>(L.c, L.ic, lane, x); R.put(2, x); }
+    }
+    // scratch: +0 to its reach, then the first n_scratch_in slots preloaded
+    uint32_t *scr = static_cast<uint32_t *>(L.scratch);
+    auto sc = [&](uint32_t slot, int w) -> uint32_t & {
+        return scr[((size_t)slot * W + w) * nl + local];
+    };
+    if (keep && scr) {
+        for (uint32_t s = 0; s < P.reach; s++) {
+#pragma unroll
+            for (int w = 0; w < W; w++) sc(s, w) = 0u;
+        }
+        if (L.scratch_in) {
+            for (uint32_t s = 0; s < P.n_scratch_in; s++) {
+                load_in<W>(L.scratch_in, L.isi, lane * P.n_scratch_in + s, x);
+#pragma unroll
+                for (int w = 0; w < W; w++) sc(s, w) = x[w];
+            }
+        }
+    }
+    uint32_t *dep = static_cast<uint32_t *>(L.deposits);
+    if (keep && dep && L.lane_mask) {
+        // with a mask the buffer holds the caller's bytes; this lane's are
+        // the run's, and start at +0
+        for (size_t k = 0; k < (size_t)P.max_deposits * W; k++)
+            dep[lane * (size_t)P.max_deposits * W + k] = 0u;
+    }
+    __syncwarp();
+
+    uint32_t count = 0, flags = 0, status = 0, err = 0;
+    uint8_t lflag = 0;
+    uint32_t body[4], left[4];
+    int sp = 0, qd = 0;
+    uint32_t pc = 0;
+    const uint32_t *kons = static_cast<const uint32_t *>(P.d_consts);
+
+    while (pc < P.n_insns) {
+        const Insn d = decode(__ldg(P.d_insns + pc));
+        if (!d.ctrl) {
+            if (active) {
+                bool ka, kb, kc;
+                const int ia = source(d, 0, ka), ib = source(d, 1, kb), ic = source(d, 2, kc);
+                uint32_t va[W], vb[W], vc[W], o[W], fl = 0u;
+                if (ka) { for (int w = 0; w < W; w++) va[w] = __ldg(kons + ia * W + w); } else R.get(ia, va);
+                if (kb) { for (int w = 0; w < W; w++) vb[w] = __ldg(kons + ib * W + w); } else R.get(ib, vb);
+                if (kc) { for (int w = 0; w < W; w++) vc[w] = __ldg(kons + ic * W + w); } else R.get(ic, vc);
+                switch (d.op) {
+                case 0: sf::arith<FMT, sf::OP_FMA>(va, vb, vc, d.rnd, o, fl); break;
+                case 1: sf::arith<FMT, sf::OP_ADD>(va, vb, vc, d.rnd, o, fl); break;
+                case 2: sf::arith<FMT, sf::OP_SUB>(va, vb, vc, d.rnd, o, fl); break;
+                case 3: sf::arith<FMT, sf::OP_MUL>(va, vb, vc, d.rnd, o, fl); break;
+                default: sf::simple<FMT>(d.op, va, vb, vc, o, fl); break;
+                }
+                R.put(reg5(d.rd, d.imm, 0), o);
+                if (!qd) {
+                    flags |= fl;
+                    lflag |= (uint8_t)fl;
+                }
+            }
+            pc++;
+            continue;
+        }
+        switch (d.op) {
+        case 0:                                              // HALT
+            pc = P.n_insns;
+            break;
+        case 1: {                                            // REPEAT
+            const bool any = __any_sync(0xFFFFFFFFu, active);
+            if (d.imm == 0u || !any) {
+                pc = (uint32_t)P.d_endrep[pc] + 1u;
+                break;
+            }
+            if (sp >= 4) { err |= 1u; pc = P.n_insns; break; }
+            body[sp] = pc + 1;
+            left[sp] = d.imm;
+            sp++;
+            pc++;
+            break;
+        }
+        case 2: {                                            // ENDREP
+            const bool any = __any_sync(0xFFFFFFFFu, active);
+            if (sp <= 0) { err |= 2u; pc = P.n_insns; break; }
+            left[sp - 1]--;
+            if (left[sp - 1] > 0u && any) {
+                pc = body[sp - 1];
+            } else {
+                sp--;
+                pc++;
+            }
+            break;
+        }
+        case 3:                                              // DEPOSIT
+            if (active) {
+                if (count >= P.max_deposits) {
+                    status |= 1u << 4;
+                    lflag |= 1u << 5;
+                } else {
+                    R.get(reg5(d.ra, d.imm, 1), x);
+                    uint32_t *p = dep + (lane * (size_t)P.max_deposits + count) * W;
+#pragma unroll
+                    for (int w = 0; w < W; w++) p[w] = x[w];
+                    count++;
+                }
+            }
+            pc++;
+            break;
+        case 4:                                              // SETACT: narrows only
+            if (active) {
+                R.get(reg5(d.ra, d.imm, 1), x);
+                x[W - 1] &= 0x7FFFFFFFu;
+                active = !sfw::is_zero(x);
+            }
+            pc++;
+            break;
+        case 5:                                              // ACTALL
+            active = keep;
+            pc++;
+            break;
+        case 6: case 7: {                                    // STL, LDL
+            const uint32_t slot = d.imm & 0x00FFFFFFu;
+            if (active) {
+                if (!scr || slot >= P.reach) {
+                    err |= 4u;
+                } else if (d.op == 6) {
+                    R.get(reg5(d.ra, d.imm, 1), x);
+#pragma unroll
+                    for (int w = 0; w < W; w++) sc(slot, w) = x[w];
+                } else {
+#pragma unroll
+                    for (int w = 0; w < W; w++) x[w] = sc(slot, w);
+                    R.put(reg5(d.rd, d.imm, 0), x);
+                }
+            }
+            pc++;
+            break;
+        }
+        case 8: case 9: {                                    // STX, LDX
+            const int rb = reg5(d.rb, d.imm, 2), rd = reg5(d.rd, d.imm, 0);
+            int step = (int)(d.imm & 0xFFFu);
+            if (step & 0x800) step -= 0x1000;
+            if (d.op == 9 && rd == rb) step = 0;             // the loaded value wins
+            if (active) {
+                uint32_t ix[W];
+                R.get(rb, ix);
+                const bool strict = (P.flags & 4u) != 0u;
+                if (strict && sfw::bitlen(ix) > (int)log2d) {
+                    status |= 1u << 5;
+                    lflag |= 1u << 6;
+                    if (d.op == 9) {
+                        sfw::zero(x);
+                        R.put(rd, x);
+                    }
+                } else {
+                    const uint32_t slot = (log2d >= 32 ? ix[0] : (ix[0] & ((1u << log2d) - 1u))) &
+                                          (P.scratch_depth - 1u);
+                    if (!scr || slot >= P.reach) {
+                        err |= 8u;
+                    } else if (d.op == 8) {
+                        R.get(reg5(d.ra, d.imm, 1), x);
+#pragma unroll
+                        for (int w = 0; w < W; w++) sc(slot, w) = x[w];
+                    } else {
+#pragma unroll
+                        for (int w = 0; w < W; w++) x[w] = sc(slot, w);
+                        R.put(rd, x);
+                    }
+                }
+                if (step) {
+                    // rb := rb +/- |step| modulo 2^width (IADD / ISUB)
+                    R.get(rb, ix);
+                    uint32_t m[W];
+                    sfw::zero(m);
+                    m[0] = (uint32_t)(step < 0 ? -step : step);
+                    if (step > 0) sfw::add(ix, ix, m);
+                    else sfw::sub(ix, ix, m);
+                    R.put(rb, ix);
+                }
+            }
+            pc++;
+            break;
+        }
+        case 12:                                             // QUIET
+            qd++;
+            pc++;
+            break;
+        case 13:                                             // ENDQUIET
+            qd--;
+            pc++;
+            break;
+        case 14:                                             // RAISE
+            if (active) {
+                R.get(reg5(d.ra, d.imm, 1), x);
+                const uint32_t low = x[0] & 0xFFu;
+                if (!qd) {
+                    flags |= low & 0x1Fu;
+                    lflag |= (uint8_t)(low & 0x1Fu);
+                }
+                if (low & 0x80u) {
+                    status |= 1u << 6;
+                    lflag |= 1u << 7;
+                }
+            }
+            pc++;
+            break;
+        default:                                             // refused at load
+            err |= 16u;
+            pc = P.n_insns;
+            break;
+        }
+    }
+
+    // outputs of the lanes the caller has (reference seq_exec.h:880-923)
+    if (keep) {
+        if (L.counts) L.counts[lane] = count;
+        if (L.lane_flags) L.lane_flags[lane] = lflag;
+        if (L.scratch_out && scr) {
+            uint32_t *so = static_cast<uint32_t *>(L.scratch_out);
+            for (uint32_t s = 0; s < P.n_scratch_out; s++) {
+#pragma unroll
+                for (int w = 0; w < W; w++) so[(lane * P.n_scratch_out + s) * W + w] = sc(s, w);
+            }
+        }
+    }
+    flags = __reduce_or_sync(0xFFFFFFFFu, flags);
+    status = __reduce_or_sync(0xFFFFFFFFu, status);
+    err = __reduce_or_sync(0xFFFFFFFFu, err);
+    if ((t & 31) == 0) {
+        if (flags) atomicOr(L.word + 0, flags);
+        if (status) atomicOr(L.word + 1, status);
+        if (err) atomicOr(L.word + 2, err);
+    }
+}
+
+template <int FMT>
+static cudaError_t go_seq(const SeqLaunch &L, cudaStream_t s)
+{
+    constexpr int W = sf::Fmt<FMT>::W;
+    const int nregs = (int)L.P.nregs;
+    const size_t per_lane = (size_t)(nregs > 0 ? nregs : 1) * W * 4;
+    int T = (int)((64u << 10) / per_lane);
+    T = (T / 32) * 32;
+    if (T > 256) T = 256;
+    if (T < 32) T = 32;
+    const size_t smem = per_lane * T;
+    cudaError_t e = cudaFuncSetAttribute(k_seq<FMT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    const size_t blocks = (L.n + T - 1) / T;
+    k_seq<FMT><<<(unsigned)blocks, T, smem, s>>>(L, 0, L.n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_seq(const SeqLaunch &L, cudaStream_t s)
+{
+    if (L.n == 0) return cudaSuccess;
+    switch (L.P.fmt) {
+    case 0: return go_seq<0>(L, s);
+    case 1: return go_seq<1>(L, s);
+    case 2: return go_seq<2>(L, s);
+    default: return go_seq<3>(L, s);
+    }
+}
+
+}  // namespace cftg

@@ -40,6 +40,12 @@ CFT_API int cftg_device_ordinal(cft_device *dev);
 /* The sequencer features this build publishes in cft_caps.seq_features. */
 CFT_API uint32_t cftg_seq_features(void);
 
+/* cft_program_load's decision over an image, taken on the host with no
+ * device: CFT_OK for an image a handle opened at scratch depth
+ * `max_scratch` (0 = 256) would load, else the status and sentence the
+ * load would give. For tools that vet images before a GPU is at hand. */
+CFT_API cft_status cftg_program_check(const void *image, size_t bytes, uint32_t max_scratch);
+
 #ifdef __cplusplus
 }
 #endif
