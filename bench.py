@@ -69,7 +69,7 @@ class Clocks:
                  "--query-gpu=clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,"
                  "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
                  "clocks_event_reasons.sw_power_cap",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "50"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -157,13 +157,15 @@ def run_reference(args):
     fmt = 3
     a, b, c = (np.ascontiguousarray(x) for x in
                __import__("cftgb.workload", fromlist=["x"]).gen_operands(fmt, 1 << 16, 1))
+    # each step is a bounded sample: the whole run stays near 90 s of host work
+    step_s = max(0.05, min(2.0, 90.0 / max(1, args.steps + args.warmup)))
     per_step = []
     for _ in range(args.warmup):
-        cpu_baseline(fmt, a, b, c, seconds=0.5)
+        cpu_baseline(fmt, a, b, c, seconds=step_s)
     total, thr = 0, 1
     t_all = 0.0
     for _ in range(args.steps):
-        rate, thr, cnt, dt = cpu_baseline(fmt, a, b, c, seconds=2.0)
+        rate, thr, cnt, dt = cpu_baseline(fmt, a, b, c, seconds=step_s)
         per_step.append(dt)
         total += cnt
         t_all += dt
@@ -173,11 +175,13 @@ def run_reference(args):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1000 * t_all / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u32-limb binary256", "data": "synthetic",
-        "config": {"workload": "binary256 FMA RNE, seeded operand mix (90% normals, 10% specials, "
-                               "cancellation triples)", "elements_per_step": "2 s of host work",
+        "config": {"workload": "binary256 FMA RNE, n=2^24 per GPU, seeded operand mix (90% "
+                               "normals exp in [-64,64], 10% specials, cancellation triples)",
+                   "elements_per_step": f"{step_s:.2f} s of host work (a bounded sample)",
                    "parallelism": "host threads"},
         "cpu_baseline": {"value": value, "unit": "Gelem/s", "cores": thr, "kind": "port",
-                         "sample": "2 s per step of 2048-element calls over 65,536 operands"},
+                         "sample": f"{step_s:.2f} s per step of 2048-element calls over the first "
+                                   "65,536 operands of the same seeded workload"},
         "e2e": {"value": value, "unit": "Gelem/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -186,8 +190,8 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
-    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=N_DEFAULT)
     ap.add_argument("--no-cpu", action="store_true")

@@ -46,6 +46,45 @@ CFT_API uint32_t cftg_seq_features(void);
  * load would give. For tools that vet images before a GPU is at hand. */
 CFT_API cft_status cftg_program_check(const void *image, size_t bytes, uint32_t max_scratch);
 
+/* ---- the batched form -------------------------------------------------
+ *
+ * Many independent elementwise calls - uneven sizes, any mix of formats,
+ * operations and rounding attributes - run as ONE persistent work-queue
+ * launch: the calls are cut into tiles, a resident grid takes tiles from
+ * one atomic counter, and each call's flags are ORed into its own device
+ * word. Every element is computed exactly as cftg_run_device computes it.
+ * A batch is prepared once (its tables live on the device) and launched
+ * any number of times; cftg_batch_capture records the launch in a CUDA
+ * graph so each replay is one graph launch. The caller keeps the operand
+ * buffers and the flag words alive while the batch exists. */
+typedef struct cftg_call {
+    int kind;                   /* CFTG_KIND_OP, _DIV or _SQRT */
+    int op;                     /* the opcode, for CFTG_KIND_OP */
+    int fmt;                    /* cft_format */
+    int rnd;                    /* cft_round */
+    const void *a, *b, *c;      /* device pointers; an unread one may be NULL */
+    void *d;                    /* device pointer, n elements */
+    size_t n;
+    uint32_t scalar_mask;       /* as cft_run_ex's */
+} cftg_call;
+
+typedef struct cftg_batch cftg_batch;
+
+CFT_API cft_status cftg_batch_create(cft_device *dev, const cftg_call *calls, size_t ncalls,
+                                     uint32_t *d_call_flags, cftg_batch **out);
+CFT_API cft_status cftg_batch_launch(cftg_batch *b, void *stream);
+CFT_API cft_status cftg_batch_capture(cftg_batch *b, void *stream);
+CFT_API void cftg_batch_free(cftg_batch *b);
+CFT_API uint32_t cftg_batch_tiles(const cftg_batch *b);
+
+/* The tile-length autotuner: times the work queue at candidate tile
+ * lengths for each format and for FMA, ADD, DIV and SQRT over n elements
+ * of the caller's device buffers (each sized for n binary256 elements),
+ * and keeps the fastest for every later batch in the process. */
+CFT_API cft_status cftg_autotune(cft_device *dev, const void *d_a, const void *d_b,
+                                 const void *d_c, void *d_d, size_t n, void *stream);
+CFT_API uint32_t cftg_tile_length(int fmt, int kind, int op);
+
 #ifdef __cplusplus
 }
 #endif

@@ -99,7 +99,8 @@ def test_lorenz63_certificate_chain(gpu):
 
 
 def test_program_info_and_digest(gpu):
-    case = su.load(su.cases()[0])
+    case = next(c for c in map(su.load, su.cases())
+                if not su.uses_augadd(c["image"]) and c["bank"].size)
     L = cftgb.lib()
     img = case["image"]
     prog = ctypes.c_void_p()
