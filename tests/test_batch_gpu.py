@@ -1,0 +1,76 @@
+"""The batched form: many uneven calls of mixed formats, operations and
+rounding attributes as one persistent work-queue launch (and as a replayed
+CUDA graph) give exactly the bits and per-call flags of one plain launch a
+call."""
+import ctypes
+
+import numpy as np
+import pytest
+
+import cftgb
+from cftgb import workload as wl
+
+pytestmark = pytest.mark.gpu
+
+
+class Call(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int), ("op", ctypes.c_int), ("fmt", ctypes.c_int),
+                ("rnd", ctypes.c_int), ("a", ctypes.c_void_p), ("b", ctypes.c_void_p),
+                ("c", ctypes.c_void_p), ("d", ctypes.c_void_p), ("n", ctypes.c_size_t),
+                ("scalar_mask", ctypes.c_uint32)]
+
+
+def test_queue_matches_plain_launches(gpu):
+    import torch
+    L = cftgb.lib()
+    vp = ctypes.c_void_p
+    L.cftg_batch_create.argtypes = [vp, ctypes.POINTER(Call), ctypes.c_size_t, vp, ctypes.POINTER(vp)]
+    L.cftg_batch_launch.argtypes = [vp, vp]
+    L.cftg_batch_capture.argtypes = [vp, vp]
+    L.cftg_batch_free.argtypes = [vp]
+    rng = np.random.default_rng(4)
+    ncalls = 300
+    calls = (Call * ncalls)()
+    keep = []
+    outs_plain, outs_q = [], []
+    plain_flags = []
+    stream = torch.cuda.current_stream().cuda_stream
+    for i in range(ncalls):
+        fmt = int(rng.choice([1, 2, 3], p=[0.2, 0.4, 0.4]))
+        n = int(np.exp(rng.uniform(0, np.log(20000))))
+        kind, op = [(0, 1), (0, 3), (0, 0), (1, 0), (2, 0)][int(rng.integers(0, 5))]
+        rnd = int(rng.integers(0, 5))
+        a, b, c = wl.gen_operands(fmt, n, 1000 + i, triples_frac=0.0)
+        ta, tb, tc = (torch.from_numpy(x.view(np.int32)).cuda() for x in (a, b, c))
+        td1, td2 = torch.zeros_like(ta), torch.zeros_like(ta)
+        fw = torch.zeros(1, dtype=torch.int32, device="cuda")
+        st = L.cftg_run_device(gpu, kind, op, fmt, rnd, ta.data_ptr(), tb.data_ptr(), tc.data_ptr(),
+                               td1.data_ptr(), n, 0, None, fw.data_ptr(), stream)
+        cftgb._lib.check(st, "cftg_run_device")
+        calls[i] = Call(kind, op, fmt, rnd, ta.data_ptr(), tb.data_ptr(), tc.data_ptr(),
+                        td2.data_ptr(), n, 0)
+        keep += [ta, tb, tc]
+        outs_plain.append(td1)
+        outs_q.append(td2)
+        plain_flags.append(fw)
+    flags = torch.zeros(ncalls, dtype=torch.int32, device="cuda")
+    b = ctypes.c_void_p()
+    cftgb._lib.check(L.cftg_batch_create(gpu, calls, ncalls, flags.data_ptr(), ctypes.byref(b)), "create")
+    cftgb._lib.check(L.cftg_batch_launch(b, stream), "launch")
+    torch.cuda.synchronize()
+    for i in range(ncalls):
+        assert torch.equal(outs_plain[i], outs_q[i]), i
+    assert torch.equal(torch.cat(plain_flags), flags)
+    # the same batch captured in a graph and replayed
+    s2 = torch.cuda.Stream()
+    for o in outs_q:
+        o.zero_()
+    flags.zero_()
+    cftgb._lib.check(L.cftg_batch_capture(b, s2.cuda_stream), "capture")
+    for _ in range(2):
+        cftgb._lib.check(L.cftg_batch_launch(b, s2.cuda_stream), "replay")
+    s2.synchronize()
+    for i in range(ncalls):
+        assert torch.equal(outs_plain[i], outs_q[i]), i
+    assert torch.equal(torch.cat(plain_flags), flags)
+    L.cftg_batch_free(b)
