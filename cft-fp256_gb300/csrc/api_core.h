@@ -85,4 +85,7 @@ bool op_is_reduction(int op);
 unsigned op_operands(int op);
 size_t esz_of(int fmt);
 
+// A loaded program's executor view and its handle (program.cpp).
+const SeqProgram *program_seq(const cft_program *pr, cft_device **dev);
+
 }  // namespace cftg

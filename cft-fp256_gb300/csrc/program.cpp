@@ -518,6 +518,15 @@ cft_status bank_rule(const cft_program *pr, const void *bank, size_t bank_bytes,
 
 }  // namespace
 
+// The loaded program as the executor reads it, and the handle it was
+// loaded on (for entry points outside this file that launch it).
+const SeqProgram *cftg::program_seq(const cft_program *pr, cft_device **dev)
+{
+    if (!pr) return nullptr;
+    if (dev) *dev = pr->dev;
+    return &pr->P;
+}
+
 extern "C" cft_status cftg_program_check(const void *image, size_t bytes, uint32_t max_scratch)
 {
     clear_error();

@@ -85,6 +85,38 @@ CFT_API cft_status cftg_autotune(cft_device *dev, const void *d_a, const void *d
                                  const void *d_c, void *d_d, size_t n, void *stream);
 CFT_API uint32_t cftg_tile_length(int fmt, int kind, int op);
 
+/* ---- a program run that allocates nothing ------------------------------
+ *
+ * No counterpart in the reference: an addition of this library. It exists
+ * for callers that cannot let a library call cudaMalloc - a host that owns
+ * every byte of device memory through its own pool or budget, or a
+ * latency-critical loop that cannot afford cudaMalloc/cudaFree's implicit
+ * device synchronisation. It runs a loaded program as cft_program_run_ex
+ * does (same bits, flags and STATUS) over DEVICE buffers the caller holds:
+ * a (n elements), b and c (n elements or NULL for +0), the bank of a
+ * BANK_EXT program, the scratch-in and scratch-out blocks of a SCRATCH_IO
+ * program (lane-major, as cft_run_args'), deposits (n * max_deposits
+ * elements, zero-filled by the call) and counts (n words, or NULL). No
+ * lane mask, index tables or per-lane flag bytes.
+ *
+ * The run's scratch - each lane's scratch slots and three flag words -
+ * comes from one fixed device array inside the library, of
+ * cftg_noalloc_scratch_bytes() usable bytes (16 MiB less 256), which every
+ * GPU that loads the library holds until exit. A run needing more (n x the
+ * program's scratch slots x the element size) is refused with
+ * CFT_ERR_INVALID_ARGUMENT and a sentence saying by how much. Every call
+ * shares the array: calls whose work overlaps on the GPU race, so issue
+ * them one after another (each returns after `stream` has finished its
+ * run). The first call on a device looks up the array's device address;
+ * make that first call before any stream capture. */
+CFT_API cft_status cftg_program_run_noalloc(cft_program *prog, const void *d_a, const void *d_b,
+                                            const void *d_c, const void *d_bank,
+                                            const void *d_scratch_in, void *d_scratch_out,
+                                            void *d_deposits, uint32_t *d_counts, size_t n,
+                                            uint32_t *flags_out, uint32_t *status_out,
+                                            void *stream);
+CFT_API size_t cftg_noalloc_scratch_bytes(void);
+
 #ifdef __cplusplus
 }
 #endif
