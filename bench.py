@@ -195,9 +195,23 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=N_DEFAULT)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--profile", action="store_true",
+                    help="only the device-resident leg (for ncu captures on a small n)")
+    ap.add_argument("--fmt", type=int, default=3, help="format of the headline leg (3 = binary256)")
+    ap.add_argument("--suite", default=None, choices=["uneven"],
+                    help="run one of the secondary configurations instead of the headline")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.suite:
+        import torch
+        import cftgb
+        from cftgb import suites
+        torch.cuda.set_device(0)
+        h = cftgb.open_device("cuda:0")
+        print(json.dumps(getattr(suites, args.suite)(h)))
+        cftgb.close_device(h)
+        return
 
     import torch
     import cftgb
@@ -213,7 +227,7 @@ def main():
     h = cftgb.open_device(f"cuda:{dev_index}")
     L = cftgb.lib()
     n = args.n
-    fmt = 3
+    fmt = args.fmt
     a, b, c = wl.gen_operands(fmt, n, 1 + rank)
     W = wl.words(fmt)
     ta, tb, tc = (torch.from_numpy(x.view(np.int32)).cuda() for x in (a, b, c))
@@ -246,6 +260,12 @@ def main():
         torch.cuda.synchronize()
     barrier()
     ms = e0.elapsed_time(e1)
+    if args.profile:
+        print(json.dumps({"profile_leg": "device-resident", "fmt": fmt, "n": n,
+                          "ms_per_launch": ms / args.steps,
+                          "gelem_s": n * args.steps / (ms / 1e3) / 1e9}))
+        cftgb.close_device(h)
+        return
     if ws > 1:
         t = torch.tensor([ms], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -254,7 +274,7 @@ def main():
     value = ws * n * args.steps / sec / 1e9
     per_launch = sec / args.steps
     hbm_peak, peak_kind = peaks()
-    alg_bytes = 4 * 32 * n
+    alg_bytes = 4 * 4 * wl.words(fmt) * n
     achieved = alg_bytes / per_launch / 1e9
 
     # correctness of what was timed: a sample against the oracle

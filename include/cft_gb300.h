@@ -85,6 +85,14 @@ CFT_API cft_status cftg_autotune(cft_device *dev, const void *d_a, const void *d
                                  const void *d_c, void *d_d, size_t n, void *stream);
 CFT_API uint32_t cftg_tile_length(int fmt, int kind, int op);
 
+/* Seeded synthetic operands written on the device: n elements of format
+ * `fmt` into d_out, 90% normals with unbiased exponents uniform in
+ * [-exp_range, exp_range], special_ppm per million specials (+-0,
+ * subnormals, +-inf, quiet and signalling NaNs, near-overflow values).
+ * Each element is a hash of (seed, index), so any range regenerates alike. */
+CFT_API cft_status cftg_fill_operands(int fmt, void *d_out, size_t n, uint64_t seed,
+                                      int exp_range, uint32_t special_ppm, void *stream);
+
 /* ---- a program run that allocates nothing ------------------------------
  *
  * No counterpart in the reference: an addition of this library. It exists
