@@ -168,3 +168,21 @@ def to_bytes(x):
 
 def from_bytes(buf, fmt):
     return np.frombuffer(buf, dtype="<u4").reshape(-1, words(fmt))
+
+
+def encode_double(fmt, x):
+    """The exact encoding of the binary64 value x in format fmt (fmt >= 1:
+    every double is representable in binary64, 128 and 256)."""
+    import struct
+    bits = struct.unpack("<Q", struct.pack("<d", float(x)))[0]
+    g = geometry(fmt)
+    sign, e, frac = bits >> 63, (bits >> 52) & 0x7FF, bits & ((1 << 52) - 1)
+    if e == 0 and frac == 0:
+        return sign << (g["width"] - 1)
+    if e == 0x7FF:
+        raise ValueError("not finite")
+    if e == 0:                                   # subnormal double
+        sig, e2 = frac, -1074
+    else:
+        sig, e2 = frac | (1 << 52), e - 1023 - 52
+    return encode(fmt, sign, sig, e2)

@@ -72,4 +72,22 @@ struct SeqLaunch {
 
 cudaError_t launch_seq(const SeqLaunch &L, cudaStream_t stream);
 
+// Many chained runs a lane (trajectories), state carried through the
+// scratch block (seq.cu, k_traj).
+struct TrajLaunch {
+    SeqProgram P;
+    size_t n = 0;
+    const void *a = nullptr, *b = nullptr, *c = nullptr;   // streams, n elements or NULL
+    const uint32_t *segments = nullptr;                      // runs a lane
+    const uint32_t *order = nullptr;                         // thread -> lane, or NULL
+    void *state = nullptr;        // n * n_scratch_out elements: the initial block in, final out
+    void *snaps = nullptr;        // n * max_snaps * n_scratch_out elements, or NULL
+    uint32_t snap_every = 0, max_snaps = 0;
+    void *scratch = nullptr;      // n * reach * esz
+    uint8_t *lane_flags = nullptr;
+    uint32_t *word = nullptr;     // [0] flags, [1] status, [2] error
+};
+
+cudaError_t launch_traj(const TrajLaunch &L, cudaStream_t stream);
+
 }  // namespace cftg

@@ -106,64 +106,33 @@ SFD void load_in(const void *src, const uint32_t *idx, size_t e, uint32_t (&x)[W
 
 }  // namespace
 
-template <int FMT>
-__global__ void k_seq(const SeqLaunch L, size_t lane0, size_t nl)
-{
-    constexpr int W = sf::Fmt<FMT>::W;
-    extern __shared__ uint32_t smem[];
-    const SeqProgram &P = L.P;
-    const int T = blockDim.x, t = threadIdx.x;
-    const size_t local = (size_t)blockIdx.x * T + t;
-    const size_t lane = lane0 + local;
-    const bool have = local < nl;
-    const int nregs = (int)P.nregs;
-    const uint32_t log2d = P.scratch_log2;
-    Lane<W> R{smem, T, t};
+// A lane's scratch slots: structure-of-words across the launch's lanes.
+template <int W>
+struct Scratch {
+    uint32_t *base;       // NULL for a program without scratch
+    size_t nl, local;     // lanes in the launch, this lane's index among them
+    SFD uint32_t &at(uint32_t slot, int w) const { return base[((size_t)slot * W + w) * nl + local]; }
+};
 
-    bool keep = have;
-    if (have && L.lane_mask) keep = (L.lane_mask[lane >> 3] >> (lane & 7)) & 1u;
-    bool active = keep;
-
-    // registers +0, then r0..r2 from the streams (reference seq_exec.h:810-860)
-    for (int r = 0; r < nregs; r++) {
-#pragma unroll
-        for (int w = 0; w < W; w++) R.at(r, w) = 0u;
-    }
-    uint32_t x[W];
-    if (keep) {
-        if (nregs > 0) { load_in<W>(L.a, L.ia, lane, x); R.put(0, x); }
-        if (nregs > 1 && L.b) { load_in<W>(L.b, L.ib, lane, x); R.put(1, x); }
-        if (nregs > 2 && L.c) { load_in<W>(L.c, L.ic, lane, x); R.put(2, x); }
-    }
-    // scratch: +0 to its reach, then the first n_scratch_in slots preloaded
-    uint32_t *scr = static_cast<uint32_t *>(L.scratch);
-    auto sc = [&](uint32_t slot, int w) -> uint32_t & {
-        return scr[((size_t)slot * W + w) * nl + local];
-    };
-    if (keep && scr) {
-        for (uint32_t s = 0; s < P.reach; s++) {
-#pragma unroll
-            for (int w = 0; w < W; w++) sc(s, w) = 0u;
-        }
-        if (L.scratch_in) {
-            for (uint32_t s = 0; s < P.n_scratch_in; s++) {
-                load_in<W>(L.scratch_in, L.isi, lane * P.n_scratch_in + s, x);
-#pragma unroll
-                for (int w = 0; w < W; w++) sc(s, w) = x[w];
-            }
-        }
-    }
-    uint32_t *dep = static_cast<uint32_t *>(L.deposits);
-    if (keep && dep && L.lane_mask) {
-        // with a mask the buffer holds the caller's bytes; this lane's are
-        // the run's, and start at +0
-        for (size_t k = 0; k < (size_t)P.max_deposits * W; k++)
-            dep[lane * (size_t)P.max_deposits * W + k] = 0u;
-    }
-    __syncwarp();
-
+// What one pass of the interpreter leaves for its lane.
+struct LaneRun {
     uint32_t count = 0, flags = 0, status = 0, err = 0;
     uint8_t lflag = 0;
+};
+
+// One run of the program for this lane (reference seq_exec.h:412-685):
+// control decided per warp, arithmetic per active lane. `active` starts as
+// the lane's keep bit; `dep` is the deposit buffer (AoS) or NULL.
+template <int FMT>
+SFD void interpret(const SeqProgram &P, const Lane<sf::Fmt<FMT>::W> &R,
+                   const Scratch<sf::Fmt<FMT>::W> &sc, uint32_t *dep, size_t lane, bool keep,
+                   bool active, LaneRun &o)
+{
+    constexpr int W = sf::Fmt<FMT>::W;
+    const uint32_t log2d = P.scratch_log2;
+    uint32_t x[W];
+    uint32_t &count = o.count, &flags = o.flags, &status = o.status, &err = o.err;
+    uint8_t &lflag = o.lflag;
     uint32_t body[4], left[4];
     int sp = 0, qd = 0;
     uint32_t pc = 0;
@@ -254,15 +223,15 @@ __global__ void k_seq(const SeqLaunch L, size_t lane0, size_t nl)
         case 6: case 7: {                                    // STL, LDL
             const uint32_t slot = d.imm & 0x00FFFFFFu;
             if (active) {
-                if (!scr || slot >= P.reach) {
+                if (!sc.base || slot >= P.reach) {
                     err |= 4u;
                 } else if (d.op == 6) {
                     R.get(reg5(d.ra, d.imm, 1), x);
 #pragma unroll
-                    for (int w = 0; w < W; w++) sc(slot, w) = x[w];
+                    for (int w = 0; w < W; w++) sc.at(slot, w) = x[w];
                 } else {
 #pragma unroll
-                    for (int w = 0; w < W; w++) x[w] = sc(slot, w);
+                    for (int w = 0; w < W; w++) x[w] = sc.at(slot, w);
                     R.put(reg5(d.rd, d.imm, 0), x);
                 }
             }
@@ -288,15 +257,15 @@ __global__ void k_seq(const SeqLaunch L, size_t lane0, size_t nl)
                 } else {
                     const uint32_t slot = (log2d >= 32 ? ix[0] : (ix[0] & ((1u << log2d) - 1u))) &
                                           (P.scratch_depth - 1u);
-                    if (!scr || slot >= P.reach) {
+                    if (!sc.base || slot >= P.reach) {
                         err |= 8u;
                     } else if (d.op == 8) {
                         R.get(reg5(d.ra, d.imm, 1), x);
 #pragma unroll
-                        for (int w = 0; w < W; w++) sc(slot, w) = x[w];
+                        for (int w = 0; w < W; w++) sc.at(slot, w) = x[w];
                     } else {
 #pragma unroll
-                        for (int w = 0; w < W; w++) x[w] = sc(slot, w);
+                        for (int w = 0; w < W; w++) x[w] = sc.at(slot, w);
                         R.put(rd, x);
                     }
                 }
@@ -344,6 +313,68 @@ __global__ void k_seq(const SeqLaunch L, size_t lane0, size_t nl)
         }
     }
 
+}
+
+template <int FMT>
+__global__ void k_seq(const SeqLaunch L, size_t lane0, size_t nl)
+{
+    constexpr int W = sf::Fmt<FMT>::W;
+    extern __shared__ uint32_t smem[];
+    const SeqProgram &P = L.P;
+    const int T = blockDim.x, t = threadIdx.x;
+    const size_t local = (size_t)blockIdx.x * T + t;
+    const size_t lane = lane0 + local;
+    const bool have = local < nl;
+    const int nregs = (int)P.nregs;
+    Lane<W> R{smem, T, t};
+
+    bool keep = have;
+    if (have && L.lane_mask) keep = (L.lane_mask[lane >> 3] >> (lane & 7)) & 1u;
+    bool active = keep;
+
+    // registers +0, then r0..r2 from the streams (reference seq_exec.h:810-860)
+    for (int r = 0; r < nregs; r++) {
+#pragma unroll
+        for (int w = 0; w < W; w++) R.at(r, w) = 0u;
+    }
+    uint32_t x[W];
+    if (keep) {
+        if (nregs > 0) { load_in<W>(L.a, L.ia, lane, x); R.put(0, x); }
+        if (nregs > 1 && L.b) { load_in<W>(L.b, L.ib, lane, x); R.put(1, x); }
+        if (nregs > 2 && L.c) { load_in<W>(L.c, L.ic, lane, x); R.put(2, x); }
+    }
+    // scratch: +0 to its reach, then the first n_scratch_in slots preloaded
+    uint32_t *scr = static_cast<uint32_t *>(L.scratch);
+    const Scratch<W> scv{scr, nl, local};
+    auto sc = [&](uint32_t slot, int w) -> uint32_t & { return scv.at(slot, w); };
+    if (keep && scr) {
+        for (uint32_t s = 0; s < P.reach; s++) {
+#pragma unroll
+            for (int w = 0; w < W; w++) sc(s, w) = 0u;
+        }
+        if (L.scratch_in) {
+            for (uint32_t s = 0; s < P.n_scratch_in; s++) {
+                load_in<W>(L.scratch_in, L.isi, lane * P.n_scratch_in + s, x);
+#pragma unroll
+                for (int w = 0; w < W; w++) sc(s, w) = x[w];
+            }
+        }
+    }
+    uint32_t *dep = static_cast<uint32_t *>(L.deposits);
+    if (keep && dep && L.lane_mask) {
+        // with a mask the buffer holds the caller's bytes; this lane's are
+        // the run's, and start at +0
+        for (size_t k = 0; k < (size_t)P.max_deposits * W; k++)
+            dep[lane * (size_t)P.max_deposits * W + k] = 0u;
+    }
+    __syncwarp();
+
+    LaneRun o;
+    interpret<FMT>(P, R, Scratch<W>{scr, nl, local}, dep, lane, keep, active, o);
+    uint32_t flags = o.flags, status = o.status, err = o.err;
+    const uint32_t count = o.count;
+    const uint8_t lflag = o.lflag;
+
     // outputs of the lanes the caller has (reference seq_exec.h:880-923)
     if (keep) {
         if (L.counts) L.counts[lane] = count;
@@ -363,6 +394,134 @@ __global__ void k_seq(const SeqLaunch L, size_t lane0, size_t nl)
         if (flags) atomicOr(L.word + 0, flags);
         if (status) atomicOr(L.word + 1, status);
         if (err) atomicOr(L.word + 2, err);
+    }
+}
+
+// Trajectories: each lane runs the program `segments[lane]` times, the
+// scratch-out block of one run feeding the scratch-in block of the next
+// (n_scratch_in == n_scratch_out), every run a complete program run as
+// cft_program_run_ex defines it (registers +0, r0..r2 from the streams,
+// scratch past the carried block +0). Lanes are visited in `order` (the host
+// sorts them by segment count, longest first, so a warp's lanes finish
+// together); a lane whose segments are done is inactive for the rest of its
+// warp's runs. Every `snap_every` runs the carried block is copied to the
+// lane's snapshot list. Flags, STATUS and the lane byte are ORed over runs.
+template <int FMT>
+__global__ void k_traj(const TrajLaunch L)
+{
+    constexpr int W = sf::Fmt<FMT>::W;
+    extern __shared__ uint32_t smem[];
+    const SeqProgram &P = L.P;
+    const int T = blockDim.x, t = threadIdx.x;
+    const size_t local = (size_t)blockIdx.x * T + t;
+    const bool have = local < L.n;
+    const size_t lane = have ? (L.order ? L.order[local] : local) : 0;
+    const uint32_t segs = have ? L.segments[lane] : 0u;
+    const int nregs = (int)P.nregs;
+    const uint32_t slots = P.n_scratch_out;
+    Lane<W> R{smem, T, t};
+    const Scratch<W> sc{static_cast<uint32_t *>(L.scratch), L.n, local};
+    uint32_t *state = static_cast<uint32_t *>(L.state);
+    uint32_t *snaps = static_cast<uint32_t *>(L.snaps);
+    uint32_t x[W];
+    if (have && sc.base) {
+        for (uint32_t s = 0; s < slots; s++) {
+#pragma unroll
+            for (int w = 0; w < W; w++) sc.at(s, w) = state[(lane * slots + s) * W + w];
+        }
+    }
+    uint32_t flags = 0, status = 0, err = 0;
+    uint8_t lflag = 0;
+    for (uint32_t seg = 0;; seg++) {
+        const bool mine = have && seg < segs;
+        if (!__any_sync(0xFFFFFFFFu, mine)) break;
+        for (int r = 0; r < nregs; r++) {
+#pragma unroll
+            for (int w = 0; w < W; w++) R.at(r, w) = 0u;
+        }
+        if (mine) {
+            if (nregs > 0) { load_in<W>(L.a, nullptr, lane, x); R.put(0, x); }
+            if (nregs > 1 && L.b) { load_in<W>(L.b, nullptr, lane, x); R.put(1, x); }
+            if (nregs > 2 && L.c) { load_in<W>(L.c, nullptr, lane, x); R.put(2, x); }
+            if (sc.base) {
+                for (uint32_t s = slots; s < P.reach; s++) {
+#pragma unroll
+                    for (int w = 0; w < W; w++) sc.at(s, w) = 0u;
+                }
+            }
+        }
+        __syncwarp();
+        LaneRun o;
+        interpret<FMT>(P, R, sc, nullptr, lane, mine, mine, o);
+        flags |= o.flags;
+        status |= o.status;
+        err |= o.err;
+        lflag |= o.lflag;
+        if (mine && snaps && L.snap_every && (seg + 1) % L.snap_every == 0) {
+            const uint32_t k = (seg + 1) / L.snap_every - 1;
+            if (k < L.max_snaps) {
+                for (uint32_t s = 0; s < slots; s++) {
+#pragma unroll
+                    for (int w = 0; w < W; w++)
+                        snaps[((lane * L.max_snaps + k) * slots + s) * W + w] = sc.at(s, w);
+                }
+            }
+        }
+    }
+    if (have) {
+        if (sc.base) {
+            for (uint32_t s = 0; s < slots; s++) {
+#pragma unroll
+                for (int w = 0; w < W; w++) state[(lane * slots + s) * W + w] = sc.at(s, w);
+            }
+        }
+        if (L.lane_flags) L.lane_flags[lane] = lflag;
+    }
+    flags = __reduce_or_sync(0xFFFFFFFFu, flags);
+    status = __reduce_or_sync(0xFFFFFFFFu, status);
+    err = __reduce_or_sync(0xFFFFFFFFu, err);
+    if ((t & 31) == 0) {
+        if (flags) atomicOr(L.word + 0, flags);
+        if (status) atomicOr(L.word + 1, status);
+        if (err) atomicOr(L.word + 2, err);
+    }
+}
+
+template <int FMT>
+static int seq_threads(const SeqProgram &P, size_t *smem)
+{
+    constexpr int W = sf::Fmt<FMT>::W;
+    const int nregs = (int)P.nregs;
+    const size_t per_lane = (size_t)(nregs > 0 ? nregs : 1) * W * 4;
+    int T = (int)((64u << 10) / per_lane);
+    T = (T / 32) * 32;
+    if (T > 256) T = 256;
+    if (T < 32) T = 32;
+    *smem = per_lane * T;
+    return T;
+}
+
+template <int FMT>
+static cudaError_t go_traj(const TrajLaunch &L, cudaStream_t s)
+{
+    size_t smem = 0;
+    const int T = seq_threads<FMT>(L.P, &smem);
+    cudaError_t e = cudaFuncSetAttribute(k_traj<FMT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    const size_t blocks = (L.n + T - 1) / T;
+    k_traj<FMT><<<(unsigned)blocks, T, smem, s>>>(L);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_traj(const TrajLaunch &L, cudaStream_t s)
+{
+    if (L.n == 0) return cudaSuccess;
+    switch (L.P.fmt) {
+    case 0: return go_traj<0>(L, s);
+    case 1: return go_traj<1>(L, s);
+    case 2: return go_traj<2>(L, s);
+    default: return go_traj<3>(L, s);
     }
 }
 

@@ -1,0 +1,64 @@
+// sf_mul.cuh - the significand product on the IMAD pipe.
+//
+// r (2N words) = a * b (N words each), operand scanning: for each word
+// a[i], one carry chain adds the low halves of a[i]*b[j] into r[i..i+N]
+// (mad.lo.cc / madc.lo.cc, then addc into r[i+N]) and a second adds the
+// high halves into r[i+1..i+N] (mad.hi.cc / madc.hi.cc). After rows 0..i
+// the partial sum is below 2^(32(i+1+N)), so r[i+N] is zero when row i
+// starts and the last high-half add carries out nothing. Each chain is one
+// asm block because the carry flag does not survive between blocks.
+#pragma once
+#include <cstdint>
+
+namespace sfw {
+
+template <int N> struct MulPtx;
+
+template <> struct MulPtx<1> {
+    static __device__ __forceinline__ void row(uint32_t *r, uint32_t a, const uint32_t (&b)[1])
+    {
+        asm("mad.lo.cc.u32 %0, %2, %3, %0;\n\taddc.u32 %1, %1, 0;\n\tmad.hi.u32 %1, %2, %3, %1;"
+            : "+r"(r[0]), "+r"(r[1])
+            : "r"(a), "r"(b[0]));
+    }
+};
+
+template <> struct MulPtx<2> {
+    static __device__ __forceinline__ void row(uint32_t *r, uint32_t a, const uint32_t (&b)[2])
+    {
+        asm("mad.lo.cc.u32 %0, %3, %4, %0;\n\tmadc.lo.cc.u32 %1, %3, %5, %1;\n\taddc.u32 %2, %2, 0;\n\tmad.hi.cc.u32 %1, %3, %4, %1;\n\tmadc.hi.u32 %2, %3, %5, %2;"
+            : "+r"(r[0]), "+r"(r[1]), "+r"(r[2])
+            : "r"(a), "r"(b[0]), "r"(b[1]));
+    }
+};
+
+template <> struct MulPtx<4> {
+    static __device__ __forceinline__ void row(uint32_t *r, uint32_t a, const uint32_t (&b)[4])
+    {
+        asm("mad.lo.cc.u32 %0, %5, %6, %0;\n\tmadc.lo.cc.u32 %1, %5, %7, %1;\n\tmadc.lo.cc.u32 %2, %5, %8, %2;\n\tmadc.lo.cc.u32 %3, %5, %9, %3;\n\taddc.u32 %4, %4, 0;\n\tmad.hi.cc.u32 %1, %5, %6, %1;\n\tmadc.hi.cc.u32 %2, %5, %7, %2;\n\tmadc.hi.cc.u32 %3, %5, %8, %3;\n\tmadc.hi.u32 %4, %5, %9, %4;"
+            : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4])
+            : "r"(a), "r"(b[0]), "r"(b[1]), "r"(b[2]), "r"(b[3]));
+    }
+};
+
+template <> struct MulPtx<8> {
+    static __device__ __forceinline__ void row(uint32_t *r, uint32_t a, const uint32_t (&b)[8])
+    {
+        asm("mad.lo.cc.u32 %0, %9, %10, %0;\n\tmadc.lo.cc.u32 %1, %9, %11, %1;\n\tmadc.lo.cc.u32 %2, %9, %12, %2;\n\tmadc.lo.cc.u32 %3, %9, %13, %3;\n\tmadc.lo.cc.u32 %4, %9, %14, %4;\n\tmadc.lo.cc.u32 %5, %9, %15, %5;\n\tmadc.lo.cc.u32 %6, %9, %16, %6;\n\tmadc.lo.cc.u32 %7, %9, %17, %7;\n\taddc.u32 %8, %8, 0;\n\tmad.hi.cc.u32 %1, %9, %10, %1;\n\tmadc.hi.cc.u32 %2, %9, %11, %2;\n\tmadc.hi.cc.u32 %3, %9, %12, %3;\n\tmadc.hi.cc.u32 %4, %9, %13, %4;\n\tmadc.hi.cc.u32 %5, %9, %14, %5;\n\tmadc.hi.cc.u32 %6, %9, %15, %6;\n\tmadc.hi.cc.u32 %7, %9, %16, %7;\n\tmadc.hi.u32 %8, %9, %17, %8;"
+            : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]), "+r"(r[8])
+            : "r"(a), "r"(b[0]), "r"(b[1]), "r"(b[2]), "r"(b[3]), "r"(b[4]), "r"(b[5]), "r"(b[6]), "r"(b[7]));
+    }
+};
+
+// r (2N words) = a * b
+template <int N>
+__device__ __forceinline__ void mul_ptx(uint32_t (&r)[2 * N], const uint32_t (&a)[N],
+                                        const uint32_t (&b)[N])
+{
+#pragma unroll
+    for (int i = 0; i < 2 * N; i++) r[i] = 0u;
+#pragma unroll
+    for (int i = 0; i < N; i++) MulPtx<N>::row(r + i, a[i], b);
+}
+
+}  // namespace sfw

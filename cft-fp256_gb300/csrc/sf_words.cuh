@@ -38,14 +38,22 @@ SFD int bitlen(const uint32_t (&x)[N])
     return L;
 }
 
+// The word-shift stages one of the active lanes needs: a stage of the
+// select network that no lane of the warp uses is skipped by the whole warp.
+SFD int warp_stages(int ws)
+{
+    return (int)__reduce_or_sync(__activemask(), (unsigned)ws);
+}
+
 // x <<= s for 0 <= s < 32N, zero fill.
 template <int N>
 SFD void shl(uint32_t (&x)[N], int s)
 {
     const int ws = s >> 5, bs = s & 31;
+    const int need = warp_stages(ws);
 #pragma unroll
     for (int b = 16; b >= 1; b >>= 1) {
-        if (b < N) {
+        if (b < N && (need & b)) {
             const bool take = (ws & b) != 0;
 #pragma unroll
             for (int i = N - 1; i >= 0; i--)
@@ -58,27 +66,22 @@ SFD void shl(uint32_t (&x)[N], int s)
 }
 
 // x >>= s with every bit shifted out ORed into bit 0 ("jamming").
-// Any s >= 0; s >= 32N leaves only the jam.
+// Any s: s <= 0 leaves x alone, s >= 32N leaves only the jam. Branch-free.
 template <int N>
 SFD void shr_jam(uint32_t (&x)[N], int s)
 {
-    if (s <= 0) return;
-    if (s >= 32 * N) {
-        const bool any = !is_zero(x);
-        zero(x);
-        x[0] = any ? 1u : 0u;
-        return;
-    }
-    const int ws = s >> 5, bs = s & 31;
+    const int sc = s <= 0 ? 0 : (s >= 32 * N ? 32 * N : s);
+    const int ws = sc >> 5, bs = sc & 31;                 // ws may be N
     uint32_t st = 0u;
 #pragma unroll
     for (int i = 0; i < N; i++) {
         const uint32_t m = (i < ws) ? 0xFFFFFFFFu : (i == ws ? ((1u << bs) - 1u) : 0u);
         st |= x[i] & m;
     }
+    const int need = warp_stages(ws);
 #pragma unroll
     for (int b = 16; b >= 1; b >>= 1) {
-        if (b < N) {
+        if (b <= N && (need & b)) {
             const bool take = (ws & b) != 0;
 #pragma unroll
             for (int i = 0; i < N; i++)
@@ -96,9 +99,10 @@ template <int N>
 SFD void shr(uint32_t (&x)[N], int s)
 {
     const int ws = s >> 5, bs = s & 31;
+    const int need = warp_stages(ws);
 #pragma unroll
     for (int b = 16; b >= 1; b >>= 1) {
-        if (b < N) {
+        if (b < N && (need & b)) {
             const bool take = (ws & b) != 0;
 #pragma unroll
             for (int i = 0; i < N; i++)

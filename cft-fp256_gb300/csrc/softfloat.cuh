@@ -21,6 +21,7 @@
 //    bits as any other exact method.
 #pragma once
 #include "sf_words.cuh"
+#include "sf_mul.cuh"
 
 namespace sf {
 
@@ -298,38 +299,61 @@ SFD void fma_general(const Unp<FMT> &ua, const Unp<FMT> &ub, const Unp<FMT> &uc,
 #pragma unroll
         for (int i = 0; i < W; i++) ma[i] = ua.m[i];
         sfw::shr_const<1>(ma);                     // leading bit at 32W-2
-        sfw::mul<W>(P, ma, ub.m);
+        sfw::mul_ptx<W>(P, ma, ub.m);
         ew = ua.ve + ub.ve - (64 * W - 3);
     }
 
     int rs = sp;
-    if (uc.cls != C_ZERO) {
+    if constexpr (OP != OP_MUL) {
+        // The addend, leading bit at 64W-2 (a zero addend stays all zero).
         uint32_t C[N];
 #pragma unroll
         for (int i = 0; i < W; i++) C[i] = 0u;
 #pragma unroll
         for (int i = 0; i < W; i++) C[W + i] = uc.m[i];
-        sfw::shr_const<1>(C);                      // leading bit at 64W-2
-        const int delta = uc.ve - (ew + 64 * W - 2);
-        if (delta > 0) {
-            sfw::shr_jam(P, delta);
-            ew += delta;
-        } else if (delta < 0) {
-            sfw::shr_jam(C, -delta);
+        sfw::shr_const<1>(C);
+        const bool czero = uc.cls == C_ZERO;
+        if (czero) {
+#pragma unroll
+            for (int i = W; i < N; i++) C[i] = 0u;
         }
-        if (sp == sc) {
-            sfw::add(P, P, C);
-        } else {
-            const uint32_t br = sfw::sub(P, P, C);
-            if (br) {
-                sfw::neg(P);
-                rs = sc;
-            }
-            if (sfw::is_zero(P)) {                 // exact cancellation
-                enc_zero<FMT>(out, rnd == RDN ? 1 : 0);
-                flags = 0u;
-                return;
-            }
+        // Branch-free alignment: Y keeps its place, X (the term with the
+        // smaller exponent) is shifted right by |delta| with jamming.
+        const int delta = czero ? -(1 << 28) : uc.ve - (ew + 64 * W - 2);
+        const bool pbig = delta <= 0;
+        uint32_t X[N], Y[N];
+#pragma unroll
+        for (int i = 0; i < N; i++) {
+            X[i] = pbig ? C[i] : P[i];
+            Y[i] = pbig ? P[i] : C[i];
+        }
+        sfw::shr_jam(X, pbig ? -delta : delta);
+        if (!pbig) ew += delta;
+        const int s_big = pbig ? sp : sc, s_small = pbig ? sc : sp;
+        // Y + X, or Y - X in two's complement, then the magnitude.
+        const bool sub = sp != sc;
+        const uint32_t mk = sub ? 0xFFFFFFFFu : 0u;
+        uint32_t cy = sub ? 1u : 0u;
+#pragma unroll
+        for (int i = 0; i < N; i++) {
+            const uint64_t t = (uint64_t)Y[i] + (X[i] ^ mk) + cy;
+            P[i] = (uint32_t)t;
+            cy = (uint32_t)(t >> 32);
+        }
+        const bool neg = sub && !cy;               // Y < X: the result is X - Y
+        const uint32_t m2 = neg ? 0xFFFFFFFFu : 0u;
+        uint32_t c2 = neg ? 1u : 0u;
+#pragma unroll
+        for (int i = 0; i < N; i++) {
+            const uint64_t t = (uint64_t)(P[i] ^ m2) + c2;
+            P[i] = (uint32_t)t;
+            c2 = (uint32_t)(t >> 32);
+        }
+        rs = neg ? s_small : s_big;
+        if (sub && sfw::is_zero(P)) {              // exact cancellation
+            enc_zero<FMT>(out, rnd == RDN ? 1 : 0);
+            flags = 0u;
+            return;
         }
     }
     round_pack<FMT, N>(rs, P, ew, rnd, out, flags);

@@ -85,6 +85,33 @@ CFT_API cft_status cftg_autotune(cft_device *dev, const void *d_a, const void *d
                                  const void *d_c, void *d_d, size_t n, void *stream);
 CFT_API uint32_t cftg_tile_length(int fmt, int kind, int op);
 
+/* ---- trajectories: the batched sequencer ------------------------------
+ *
+ * Thousands of lanes of one program, each run `segments[lane]` times in a
+ * row with its scratch-out block fed back as the next run's scratch-in
+ * (programs whose scratch blocks are equal in and out and that deposit
+ * nothing, e.g. the ODE segment programs), as ONE launch. Every run is a
+ * complete run as cft_program_run_ex defines it, so each lane's states are
+ * those a host loop of single runs would produce. d_state holds n x
+ * n_scratch_out elements, lane-major: the initial block in, the final block
+ * out. With d_snaps, every snap_every runs the block is also copied to
+ * d_snaps[(lane * max_snaps + k) * n_scratch_out ...] for k = runs /
+ * snap_every - 1 < max_snaps. Flags, STATUS and the per-lane flag byte are
+ * ORed over every run. `segments` is a HOST array read at creation (lanes
+ * are ordered longest first so a warp's lanes finish together). Device
+ * pointers otherwise; the caller keeps them alive. */
+typedef struct cftg_traj cftg_traj;
+CFT_API cft_status cftg_traj_create(cft_program *prog, const uint32_t *segments, size_t n,
+                                    const void *d_a, const void *d_b, const void *d_c,
+                                    const void *d_bank, void *d_state, void *d_snaps,
+                                    uint32_t snap_every, uint32_t max_snaps,
+                                    uint8_t *d_lane_flags, cftg_traj **out);
+CFT_API cft_status cftg_traj_launch(cftg_traj *t, void *stream);
+CFT_API cft_status cftg_traj_capture(cftg_traj *t, void *stream);
+CFT_API cft_status cftg_traj_result(cftg_traj *t, uint32_t *flags_out, uint32_t *status_out,
+                                    void *stream);
+CFT_API void cftg_traj_free(cftg_traj *t);
+
 /* Seeded synthetic operands written on the device: n elements of format
  * `fmt` into d_out, 90% normals with unbiased exponents uniform in
  * [-exp_range, exp_range], special_ppm per million specials (+-0,

@@ -1,0 +1,105 @@
+"""The batched sequencer (cftg_traj_*): uneven trajectories of the fp256
+Lorenz-63 RK4 segment program as one launch (and as a replayed graph),
+against the oracle running the same segments one run at a time, and
+against the reference's certificate for three segments."""
+import ctypes
+import hashlib
+
+import numpy as np
+import pytest
+
+import cftgb
+import oracle_lib
+import seq_util as su
+from cftgb import workload as wl
+
+pytestmark = pytest.mark.gpu
+TAG = b"cft-certificate 1 state\0"
+
+
+def _bind(L):
+    vp = ctypes.c_void_p
+    L.cftg_traj_create.argtypes = [vp, vp, ctypes.c_size_t, vp, vp, vp, vp, vp, vp,
+                                   ctypes.c_uint32, ctypes.c_uint32, vp, ctypes.POINTER(vp)]
+    L.cftg_traj_launch.argtypes = [vp, vp]
+    L.cftg_traj_capture.argtypes = [vp, vp]
+    L.cftg_traj_result.argtypes = [vp, vp, vp, vp]
+    L.cftg_traj_free.argtypes = [vp]
+
+
+def _traj(h, img, bank, state, segs, snap_every, max_snaps, graph=False):
+    import torch
+    L = cftgb.lib()
+    _bind(L)
+    n = len(segs)
+    prog = ctypes.c_void_p()
+    cftgb._lib.check(L.cft_program_load(h, img.ctypes.data, img.size, ctypes.byref(prog)), "load")
+    W = state.shape[1]
+    ta = torch.zeros((n, W), dtype=torch.int32, device="cuda")
+    tbank = torch.from_numpy(bank.view(np.int32).copy()).cuda()
+    tstate = torch.from_numpy(state.view(np.int32).copy()).cuda()
+    slots = state.shape[0] // n
+    tsnap = torch.zeros((n * max_snaps * slots, W), dtype=torch.int32, device="cuda")
+    tlf = torch.zeros(n, dtype=torch.uint8, device="cuda")
+    sg = np.asarray(segs, np.uint32)
+    t = ctypes.c_void_p()
+    cftgb._lib.check(L.cftg_traj_create(prog, sg.ctypes.data, n, ta.data_ptr(), None, None,
+                                        tbank.data_ptr(), tstate.data_ptr(), tsnap.data_ptr(),
+                                        snap_every, max_snaps, tlf.data_ptr(), ctypes.byref(t)),
+                     "cftg_traj_create")
+    s = torch.cuda.Stream()
+    if graph:
+        cftgb._lib.check(L.cftg_traj_capture(t, s.cuda_stream), "capture")
+    cftgb._lib.check(L.cftg_traj_launch(t, s.cuda_stream), "launch")
+    fl, st = ctypes.c_uint32(), ctypes.c_uint32()
+    cftgb._lib.check(L.cftg_traj_result(t, ctypes.byref(fl), ctypes.byref(st), s.cuda_stream), "result")
+    L.cftg_traj_free(t)
+    L.cft_program_free(prog)
+    return (tstate.cpu().numpy().view(np.uint32), tsnap.cpu().numpy().view(np.uint32),
+            tlf.cpu().numpy(), fl.value, st.value)
+
+
+def test_certificate_segments_as_one_trajectory_launch(gpu):
+    z = np.load(su.GOLD / "lorenz63_cert.npz")
+    state = z["state0"].copy().view(np.uint32).reshape(-1, 8)
+    n = state.shape[0] // 3
+    segs = [len(z["ends"])] * n
+    final, snaps, lf, fl, st = _traj(gpu, z["image"].copy(), z["bank"].copy(), state, segs, 1, 3)
+    snaps = snaps.reshape(n, 3, 3, 8)
+    for k, end in enumerate(z["ends"]):
+        blk = snaps[:, k].reshape(-1, 8)          # lane-major block after segment k
+        assert hashlib.sha256(TAG + blk.tobytes()).hexdigest() == str(end), k
+    assert hashlib.sha256(TAG + final.tobytes()).hexdigest() == str(z["ends"][-1])
+    assert fl == int(np.bitwise_or.reduce(z["flags"])) and st == 0
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_uneven_trajectories_match_oracle(gpu, oracle, graph):
+    z = np.load(su.GOLD / "lorenz63_cert.npz")
+    img, bank = z["image"].copy(), z["bank"].copy()
+    rng = np.random.default_rng(5)
+    n = 37
+    init = np.zeros((n * 3, 8), np.uint32)
+    for i in range(n):
+        for j in range(3):
+            init[i * 3 + j] = wl.from_int(wl.encode_double(3, 1.0 + rng.normal(0, 1e-3)), 8)
+    segs = rng.integers(1, 7, n).tolist()
+    final, snaps, lf, fl, st = _traj(gpu, img, bank, init, segs, 2, 3, graph=graph)
+    snaps = snaps.reshape(n, 3, 3, 8)
+    # the oracle: each lane's segments one run at a time
+    acc = 0
+    for i in range(n):
+        s = init[i * 3:(i + 1) * 3].copy()
+        for k in range(segs[i]):
+            out = np.zeros_like(s)
+            A = oracle_lib.SeqArgs()
+            a = np.zeros((1, 8), np.uint32)
+            A.a, A.n, A.bank = a.ctypes.data, 1, bank.ctypes.data
+            A.scratch_in, A.scratch_out, A.depth = s.ctypes.data, out.ctypes.data, 256
+            assert oracle.L.sfp_seq_run(img.ctypes.data, img.size, ctypes.byref(A)) == 0
+            acc |= A.flags_out
+            s = out
+            if (k + 1) % 2 == 0:
+                assert np.array_equal(snaps[i, (k + 1) // 2 - 1], s), (i, k)
+        assert np.array_equal(final[i * 3:(i + 1) * 3], s), i
+    assert fl == acc
