@@ -198,6 +198,8 @@ def main():
     ap.add_argument("--profile", action="store_true",
                     help="only the device-resident leg (for ncu captures on a small n)")
     ap.add_argument("--fmt", type=int, default=3, help="format of the headline leg (3 = binary256)")
+    ap.add_argument("--op", default="fma", choices=["fma", "add", "mul", "div", "sqrt"],
+                    help="operation of the --profile leg")
     ap.add_argument("--suite", default=None, choices=["uneven"],
                     help="run one of the secondary configurations instead of the headline")
     args = ap.parse_args()
@@ -235,8 +237,11 @@ def main():
     tf = torch.zeros(1, dtype=torch.int32, device="cuda")
     stream = torch.cuda.current_stream()
 
+    kind_op = {"fma": (0, 0), "add": (0, 1), "mul": (0, 3), "div": (1, 0), "sqrt": (2, 0)}
+    pkind, pop = kind_op[args.op] if args.profile else (0, 0)
+
     def launch(fmt_, A, B, C, D, nn):
-        st = L.cftg_run_device(h, 0, 0, fmt_, 0, A.data_ptr(), B.data_ptr(), C.data_ptr(),
+        st = L.cftg_run_device(h, pkind, pop, fmt_, 0, A.data_ptr(), B.data_ptr(), C.data_ptr(),
                                D.data_ptr(), nn, 0, None, tf.data_ptr(), stream.cuda_stream)
         if st:
             cftgb._lib.check(st, "cftg_run_device")
@@ -261,7 +266,7 @@ def main():
     barrier()
     ms = e0.elapsed_time(e1)
     if args.profile:
-        print(json.dumps({"profile_leg": "device-resident", "fmt": fmt, "n": n,
+        print(json.dumps({"profile_leg": "device-resident", "fmt": fmt, "op": args.op, "n": n,
                           "ms_per_launch": ms / args.steps,
                           "gelem_s": n * args.steps / (ms / 1e3) / 1e9}))
         cftgb.close_device(h)

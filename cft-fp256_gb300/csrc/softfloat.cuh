@@ -15,8 +15,9 @@
 //  * round_pack: normalise the window to its top bit with one variable
 //    shift, read kept/guard/sticky at fixed positions, and denormalise only
 //    for results below the normal range.
-//  * div: restoring long division to p+4 quotient bits plus a remainder
-//    sticky; sqrt: the digit-by-digit integer root to p+3 bits plus sticky.
+//  * div: base-2^32 long division (Knuth's Algorithm D) to at least p+3
+//    quotient bits plus a remainder sticky; sqrt: the base-2^32
+//    digit-by-digit integer root to at least p+3 bits plus sticky.
 //    Both are exact quotient/root computations, so they round to the same
 //    bits as any other exact method.
 #pragma once
@@ -421,6 +422,82 @@ SFD void arith(const uint32_t (&x)[Fmt<FMT>::W], const uint32_t (&y)[Fmt<FMT>::W
     fma_general<FMT, OP>(ua, ub, uc, uc.sign, rnd, out, flags);
 }
 
+// ---- exact division of significands ---------------------------------------
+
+// q (W+1 words) = floor(X * 2^(32W) / Y) and rnz = (remainder != 0), for X, Y
+// of W words with their top bits set. Base-2^32 long division (Knuth,
+// TAOCP vol. 2, 4.3.1, Algorithm D): each quotient digit is estimated from
+// the top two remainder words over Y's top word, refined against Y's second
+// word, and fixed by at most one add-back after the multiply-subtract.
+template <int W>
+SFD void divrem_top(const uint32_t (&X)[W], const uint32_t (&Y)[W], uint32_t (&q)[W + 1],
+                    uint32_t &rnz)
+{
+    if constexpr (W == 1) {
+        const uint64_t u = (uint64_t)X[0] << 32;
+        const uint64_t qq = u / Y[0];
+        q[0] = (uint32_t)qq;
+        q[1] = (uint32_t)(qq >> 32);
+        rnz = (uint32_t)(u - qq * Y[0]) != 0u;
+    } else {
+        constexpr int n = W, m = W;             // divisor words, quotient digits - 1
+        uint32_t u[m + n + 1];                  // X * 2^(32W), one spare top word
+#pragma unroll
+        for (int i = 0; i < n; i++) u[i] = 0u;
+#pragma unroll
+        for (int i = 0; i < n; i++) u[n + i] = X[i];
+        u[m + n] = 0u;
+        const uint32_t vt = Y[n - 1], vs = Y[n - 2];
+#pragma unroll
+        for (int j = m; j >= 0; j--) {
+            const uint64_t num = ((uint64_t)u[j + n] << 32) | u[j + n - 1];
+            uint64_t qhat, rhat;
+            if (u[j + n] >= vt) {
+                qhat = 0xFFFFFFFFull;
+                rhat = num - qhat * vt;
+            } else {
+                qhat = num / vt;
+                rhat = num - qhat * vt;
+            }
+            // at most two corrections make qhat exact or one too large
+            for (int k = 0; k < 2; k++) {
+                if (rhat <= 0xFFFFFFFFull && qhat * vs > ((rhat << 32) | u[j + n - 2])) {
+                    qhat--;
+                    rhat += vt;
+                }
+            }
+            // u[j .. j+n] -= qhat * Y
+            uint32_t carry = 0u, borrow = 0u;
+#pragma unroll
+            for (int i = 0; i < n; i++) {
+                const uint64_t p = qhat * Y[i] + carry;
+                carry = (uint32_t)(p >> 32);
+                const uint64_t t = (uint64_t)u[i + j] - (uint32_t)p - borrow;
+                u[i + j] = (uint32_t)t;
+                borrow = (uint32_t)(t >> 63);
+            }
+            const uint64_t t = (uint64_t)u[j + n] - carry - borrow;
+            u[j + n] = (uint32_t)t;
+            if (t >> 63) {                        // one too large: add Y back
+                qhat--;
+                uint32_t c = 0u;
+#pragma unroll
+                for (int i = 0; i < n; i++) {
+                    const uint64_t a2 = (uint64_t)u[i + j] + Y[i] + c;
+                    u[i + j] = (uint32_t)a2;
+                    c = (uint32_t)(a2 >> 32);
+                }
+                u[j + n] += c;
+            }
+            q[j] = (uint32_t)qhat;
+        }
+        uint32_t o = 0u;
+#pragma unroll
+        for (int i = 0; i < n; i++) o |= u[i];
+        rnz = o != 0u;
+    }
+}
+
 // ---- division (definition: python/cft_golden/softfloat.py:440-471) ------
 
 template <int FMT>
@@ -453,44 +530,127 @@ SFD void div(const uint32_t (&x)[Fmt<FMT>::W], const uint32_t (&y)[Fmt<FMT>::W],
     }
     if (ua.cls == C_ZERO) { enc_zero<FMT>(out, sq); return; }
 
-    // Both significands have their leading bit at 32W-1. Restoring division
-    // of X by Y produces Q = P+4 quotient bits; the first may be zero, so at
-    // least P+3 are significant. The remainder r < Y always, and r << 1 may
-    // need bit 32W: kept in `top`.
-    constexpr int Q = F::P + 4;
-    constexpr int NQ = (Q + 1 + 31) / 32;          // quotient + sticky bit
-    uint32_t r[W], q[NQ];
+    // Both significands have their leading bit at 32W-1. The quotient of
+    // X * 2^(32W) by Y, exact with its remainder, by long division in base
+    // 2^32 (Knuth, TAOCP vol. 2, 4.3.1, Algorithm D; Y is already
+    // normalised). Q has W+1 words and at least 32W >= P+3 significant
+    // bits, since X/Y > 1/2.
+    uint32_t q[W + 1], rnz;
+    divrem_top<W>(ua.m, ub.m, q, rnz);
+    // fold the remainder in as a sticky bit below the quotient
+    uint32_t m[W + 1];
 #pragma unroll
-    for (int i = 0; i < W; i++) r[i] = ua.m[i];
-    sfw::zero(q);
-    uint32_t top = 0u;
-#pragma unroll 1
-    for (int k = 0; k < Q; k++) {
-        uint32_t t[W];
-        const uint32_t br = sfw::sub(t, r, ub.m);
-        const bool ge = top || !br;
-        if (ge) {
+    for (int i = W; i >= 1; i--) m[i] = __funnelshift_l(q[i - 1], q[i], 1);
+    m[0] = (q[0] << 1) | (rnz ? 1u : 0u);
+    // |a/b| = (X/Y) 2^(ve_a - ve_b) = Q 2^(ve_a - ve_b - 32W) (+ remainder)
+    const int e = ua.ve - ub.ve - 32 * W - 1;
+    round_pack<FMT, W + 1>(sq, m, e, rnd, out, flags);
+}
+
+// ---- exact integer square root of a significand ----------------------------
+
+// floor(sqrt(t)) for t < 2^64, bit by bit.
+SFD uint32_t isqrt64(uint64_t t)
+{
+    uint32_t r = 0u;
 #pragma unroll
-            for (int i = 0; i < W; i++) r[i] = t[i];
-        }
-        // q = (q << 1) | ge
-#pragma unroll
-        for (int i = NQ - 1; i >= 1; i--) q[i] = __funnelshift_l(q[i - 1], q[i], 1);
-        q[0] = (q[0] << 1) | (ge ? 1u : 0u);
-        // r <<= 1 (skipped after the last digit)
-        top = r[W - 1] >> 31;
-#pragma unroll
-        for (int i = W - 1; i >= 1; i--) r[i] = __funnelshift_l(r[i - 1], r[i], 1);
-        r[0] <<= 1;
+    for (int b = 31; b >= 0; b--) {
+        const uint32_t c = r | (1u << b);
+        if ((uint64_t)c * c <= t) r = c;
     }
-    // After the loop r holds 2*rem (and top its overflow); any non-zero is sticky.
-    const bool rem = top || !sfw::is_zero(r);
+    return r;
+}
+
+// S (W words) = floor(sqrt(N)) and rnz = (N != S^2), for N of 2W words with
+// N >= 2^(64W-2). Digit by digit in base B = 2^32, the pencil-and-paper
+// method: the first digit is the exact root of N's top 64 bits; each next
+// digit d is the largest with (2rB + d) d <= rem, where r is the root so
+// far and rem = (N's prefix) - r^2. Its estimate is floor(rem / (2rB))
+// taken from the top words (r is normalised: its top bit is set), which is
+// never below d and at most three above it, so at most three add-backs of
+// (2rB + 2d + 1) correct it.
+template <int W>
+SFD void isqrtrem(const uint32_t (&N)[2 * W], uint32_t (&S)[W], uint32_t &rnz)
+{
+    constexpr int RW = W + 2;                // remainder words
+    uint32_t rem[RW], r[W + 1];
 #pragma unroll
-    for (int i = NQ - 1; i >= 1; i--) q[i] = __funnelshift_l(q[i - 1], q[i], 1);
-    q[0] = (q[0] << 1) | (rem ? 1u : 0u);
-    // value = q * 2^e: the first quotient bit has weight 2^(ve_a - ve_b)
-    const int e = ua.ve - ub.ve - Q;
-    round_pack<FMT, NQ>(sq, q, e, rnd, out, flags);
+    for (int i = 0; i < RW; i++) rem[i] = 0u;
+#pragma unroll
+    for (int i = 0; i <= W; i++) r[i] = 0u;
+    {
+        const uint64_t t = ((uint64_t)N[2 * W - 1] << 32) | N[2 * W - 2];
+        const uint32_t d = isqrt64(t);                         // >= 2^31
+        const uint64_t e = t - (uint64_t)d * d;                // <= 2d < 2^33
+        rem[0] = (uint32_t)e;
+        rem[1] = (uint32_t)(e >> 32);
+        r[0] = d;
+    }
+#pragma unroll
+    for (int i = 1; i < W; i++) {
+        // rem = rem * B^2 + the next two words of N  (rem < (2r + 1) B^2)
+#pragma unroll
+        for (int j = RW - 1; j >= 2; j--) rem[j] = rem[j - 2];
+        rem[1] = N[2 * W - 1 - 2 * i];
+        rem[0] = N[2 * W - 2 - 2 * i];
+        // estimate floor(rem / (2 r B)) = floor((rem >> 1) / (r B)) from the
+        // top two words of rem >> 1 over r's top word (r[i-1] >= 2^31)
+        const uint32_t u1 = __funnelshift_r(rem[i + 1], rem[i + 2], 1);
+        const uint32_t u0 = __funnelshift_r(rem[i], rem[i + 1], 1);
+        const uint32_t rt = r[i - 1];
+        uint32_t d = 0xFFFFFFFFu;
+        if (u1 < rt) {
+            const uint64_t qq = (((uint64_t)u1 << 32) | u0) / rt;
+            d = qq > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)qq;
+        }
+        // D = 2 r B + d (words: d, then 2r)
+        uint32_t D[RW];
+        D[0] = d;
+#pragma unroll
+        for (int j = 1; j < RW; j++) {
+            const uint32_t hi = (j - 1 <= W) ? r[j - 1] : 0u;
+            const uint32_t lo = (j >= 2 && j - 2 <= W) ? r[j - 2] : 0u;
+            D[j] = __funnelshift_l(lo, hi, 1);
+        }
+        // rem -= D * d   (D * d < B^(i+3) <= B^RW: no carry out)
+        uint32_t carry = 0u, borrow = 0u;
+#pragma unroll
+        for (int j = 0; j < RW; j++) {
+            const uint64_t pj = (uint64_t)D[j] * d + carry;
+            carry = (uint32_t)(pj >> 32);
+            const uint64_t tj = (uint64_t)rem[j] - (uint32_t)pj - borrow;
+            rem[j] = (uint32_t)tj;
+            borrow = (uint32_t)(tj >> 63);
+        }
+        // the estimate is never low and at most three high: while rem < 0,
+        // d -= 1 and rem += 2 r B + 2 d + 1
+        bool neg = borrow != 0u;
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            if (neg) {
+                d -= 1u;
+                uint32_t c = 0u;
+#pragma unroll
+                for (int j = 0; j < RW; j++) {
+                    const uint32_t add = j == 0 ? (d << 1) | 1u : j == 1 ? D[1] + (d >> 31) : D[j];
+                    const uint64_t a2 = (uint64_t)rem[j] + add + c;
+                    rem[j] = (uint32_t)a2;
+                    c = (uint32_t)(a2 >> 32);
+                }
+                neg = c == 0u;
+            }
+        }
+        // r = r B + d
+#pragma unroll
+        for (int j = W; j >= 1; j--) r[j] = r[j - 1];
+        r[0] = d;
+    }
+#pragma unroll
+    for (int i = 0; i < W; i++) S[i] = r[i];
+    uint32_t o = 0u;
+#pragma unroll
+    for (int i = 0; i < RW; i++) o |= rem[i];
+    rnz = o != 0u;
 }
 
 // ---- square root (definition: python/cft_golden/softfloat.py:474-505) ---
@@ -520,74 +680,28 @@ SFD void sqrt(const uint32_t (&x)[Fmt<FMT>::W], int rnd, uint32_t (&out)[Fmt<FMT
         for (int i = 0; i < W; i++) out[i] = x[i];
         return;
     }
-    // Radicand: the significand (leading bit at 32W-1, value m * 2^(ve-32W+1))
-    // shifted so its exponent is even and the root has R = P+3 bits. Let the
-    // radicand X = m_top * 2^(k) as a 2R-bit integer with X in [2^(2R-2), 2^(2R)).
-    constexpr int R = F::P + 3;
-    constexpr int NX = (2 * R + 31) / 32;           // radicand words
-    constexpr int NR = (R + 1 + 31) / 32;           // root + sticky
-    // exponent of the radicand's bit 0 must be even; place m's leading bit at
-    // bit 2R-1 or 2R-2 accordingly.
-    uint32_t X[NX];
-    sfw::zero(X);
-    // leading bit position in X: 2R-1 if (ve - (2R-1)) is even, else 2R-2
-    const int lead = ((ua.ve - (2 * R - 1)) & 1) ? (2 * R - 2) : (2 * R - 1);
-    const int ex = ua.ve - lead;                     // even
-    {
-        // place ua.m (leading bit 32W-1) so its leading bit is at `lead`
-        uint32_t t[NX];
-        sfw::zero(t);
-        constexpr int OFF = NX - W;                 // put m in the top W words
+    // The radicand N: the significand (leading bit at 32W-1) placed in 2W
+    // words with its leading bit at 64W-1 or 64W-2, whichever leaves the
+    // exponent of N's bit 0 even. Its root S = floor(sqrt(N)) then has
+    // exactly 32W >= P+3 bits (N >= 2^(64W-2)).
+    uint32_t N[2 * W];
 #pragma unroll
-        for (int i = 0; i < W; i++) t[OFF + i] = ua.m[i];
-        // leading bit is now at 32NX-1; shift right to `lead` (no bits lost:
-        // the significand has P <= 2R - 32(NX - W) ... enough low zeros)
-        sfw::shr_jam(t, 32 * NX - 1 - lead);
+    for (int i = 0; i < W; i++) N[i] = 0u;
 #pragma unroll
-        for (int i = 0; i < NX; i++) X[i] = t[i];
-    }
-    // digit-by-digit root: R iterations over bit pairs from the top
-    uint32_t rem[NX], res[NX];
-    sfw::zero(rem);
-    sfw::zero(res);
-#pragma unroll 1
-    for (int k = R - 1; k >= 0; k--) {
-        // rem = (rem << 2) | X[2k+1:2k]
-        const int bp = 2 * k;
-        uint32_t two = 0u;
+    for (int i = 0; i < W; i++) N[W + i] = ua.m[i];          // leading bit at 64W-1
+    // N = m_top * 2^(ve - 64W + 1); make that exponent even
+    const bool odd = ((ua.ve - 64 * W + 1) & 1) != 0;
+    if (odd) sfw::shr_const<1>(N);                             // leading bit at 64W-2
+    const int ex = ua.ve - 64 * W + 1 + (odd ? 1 : 0);         // even
+    uint32_t S[W], rnz;
+    isqrtrem<W>(N, S, rnz);
+    uint32_t m[W + 1];
+    m[W] = S[W - 1] >> 31;
 #pragma unroll
-        for (int i = 0; i < NX; i++)
-            if (i == (bp >> 5)) two = (X[i] >> (bp & 31)) & 3u;
-#pragma unroll
-        for (int i = NX - 1; i >= 1; i--) rem[i] = __funnelshift_l(rem[i - 1], rem[i], 2);
-        rem[0] = (rem[0] << 2) | two;
-        // trial = (res << 2) | 1
-        uint32_t tr[NX];
-#pragma unroll
-        for (int i = NX - 1; i >= 1; i--) tr[i] = __funnelshift_l(res[i - 1], res[i], 2);
-        tr[0] = (res[0] << 2) | 1u;
-        uint32_t d[NX];
-        const uint32_t br = sfw::sub(d, rem, tr);
-#pragma unroll
-        for (int i = NX - 1; i >= 1; i--) res[i] = __funnelshift_l(res[i - 1], res[i], 1);
-        res[0] <<= 1;
-        if (!br) {
-#pragma unroll
-            for (int i = 0; i < NX; i++) rem[i] = d[i];
-            res[0] |= 1u;
-        }
-    }
-    // res has R bits (leading bit set since X >= 2^(2R-2)); fold sticky
-    uint32_t m[NR];
-#pragma unroll
-    for (int i = 0; i < NR; i++) m[i] = 0u;
-#pragma unroll
-    for (int i = 0; i < NR && i < NX; i++) m[i] = res[i];
-#pragma unroll
-    for (int i = NR - 1; i >= 1; i--) m[i] = __funnelshift_l(m[i - 1], m[i], 1);
-    m[0] = (m[0] << 1) | (sfw::is_zero(rem) ? 0u : 1u);
-    // root value = res * 2^(ex/2); m = 2*res + sticky -> exponent ex/2 - 1
-    round_pack<FMT, NR>(0, m, (ex >> 1) - 1, rnd, out, flags);
+    for (int i = W - 1; i >= 1; i--) m[i] = __funnelshift_l(S[i - 1], S[i], 1);
+    m[0] = (S[0] << 1) | (rnz ? 1u : 0u);
+    // sqrt(|x|) = sqrt(N) 2^(ex/2); m = 2S + sticky
+    round_pack<FMT, W + 1>(0, m, (ex >> 1) - 1, rnd, out, flags);
 }
 
 }  // namespace sf
