@@ -237,6 +237,15 @@ static cft_status open_impl(const char *who, const char *artifact, int index, ui
     if (!dev) return CFT_ERR_OUT_OF_MEMORY;
     dev->ordinal = ord;
     dev->max_scratch = depth ? depth : 256u;
+    {
+        int v = 0;
+        if (cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccessUsesHostPageTables, ord) !=
+            cudaSuccess) {
+            cudaGetLastError();
+            v = 0;
+        }
+        dev->host_page_tables = v;
+    }
     bool ok = cudaStreamCreateWithFlags(&dev->s[0], cudaStreamNonBlocking) == cudaSuccess &&
               cudaStreamCreateWithFlags(&dev->s[1], cudaStreamNonBlocking) == cudaSuccess &&
               cudaMalloc(&dev->d_word, 64 * sizeof(uint32_t)) == cudaSuccess &&
@@ -602,6 +611,83 @@ bool windows_overlap(const void *a, size_t an, const void *b, size_t bn)
 
 }  // namespace
 
+// The kernels load an element as 4-, 8- or 16-byte vectors, so an operand
+// must start on that boundary; anything else is staged through aligned
+// device memory by cudaMemcpy, which takes any alignment.
+static bool aligned_for(const void *p, size_t esz)
+{
+    const uintptr_t a = esz >= 16 ? 16 : esz;
+    return ((uintptr_t)p % a) == 0;
+}
+
+// A pointer a kernel can dereference for the caller's host memory, or NULL:
+// pinned host memory through its mapped device pointer, and on a system
+// whose GPU walks the host page tables (Grace's NVLink-C2C with ATS) any
+// host pointer as it is.
+static const void *device_view(cft_device *dev, const void *p, size_t esz)
+{
+    if (!p || !aligned_for(p, esz)) return nullptr;
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    const void *v = nullptr;
+    if ((at.type == cudaMemoryTypeHost || at.type == cudaMemoryTypeDevice ||
+         at.type == cudaMemoryTypeManaged) && at.devicePointer)
+        v = at.devicePointer;
+    else if (at.type == cudaMemoryTypeUnregistered && dev->host_page_tables)
+        v = p;
+    return (v && aligned_for(v, esz)) ? v : nullptr;
+}
+
+// The direct route: every operand and the output are reachable by the
+// kernel where they are, so one launch reads and writes them in place (no
+// staging copies; the host link carries only the bytes the kernel touches).
+static bool exec_direct(const char *who, cft_device *dev, int kind, int op, int fmt, int rnd,
+                        const void *const opnd[3], void *d, size_t n, uint32_t scalar_mask,
+                        uint32_t *flags_out, cft_status *st)
+{
+    const size_t esz = esz_of(fmt);
+    const char *mode = getenv("CFTG_HOST_ACCESS");
+    if (mode && strcmp(mode, "stage") == 0) return false;
+    const void *v[3] = {nullptr, nullptr, nullptr};
+    for (int r = 0; r < 3; r++) {
+        if (!opnd[r]) continue;
+        if (find_buffer(dev, opnd[r], esz, nullptr)) return false;
+        v[r] = device_view(dev, opnd[r], esz);
+        if (!v[r]) return false;
+    }
+    if (find_buffer(dev, d, esz, nullptr)) return false;
+    void *vd = const_cast<void *>(device_view(dev, d, esz));
+    if (!vd) return false;
+    cudaStream_t s = dev->s[0];
+    ElemLaunch L;
+    L.fmt = fmt;
+    L.kind = kind;
+    L.op = op;
+    L.rnd = rnd;
+    L.a = v[0];
+    L.b = v[1];
+    L.c = v[2];
+    L.d = vd;
+    L.n = n;
+    L.scalar_mask = scalar_mask & 7u;
+    L.flags = dev->d_word;
+    cudaError_t e = cudaMemsetAsync(dev->d_word, 0, sizeof(uint32_t), s);
+    if (e == cudaSuccess) e = launch_elem(L, s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(dev->h_word, dev->d_word, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        *st = poison(dev, who, e);
+        return true;
+    }
+    flags_emit(dev, dev->h_word[0] & CFT_FLAGS_ALL, flags_out);
+    *st = CFT_OK;
+    return true;
+}
+
 // One elementwise run after the reference's argument checks have passed.
 static cft_status exec_elem(const char *who, cft_device *dev, int kind, int op, int fmt, int rnd,
                             const void *a, const void *b, const void *c, void *d, size_t n,
@@ -613,6 +699,13 @@ static cft_status exec_elem(const char *who, cft_device *dev, int kind, int op, 
     const unsigned need = (kind == K_DIV) ? 3u : (kind == K_SQRT) ? 1u : op_operands(op);
     Operand o[3];
     const void *ptr[3] = {a, b, c};
+    if (!idx) {
+        const void *read[3];
+        for (int r = 0; r < 3; r++) read[r] = ((need >> r) & 1u) ? ptr[r] : nullptr;
+        cft_status st;
+        if (exec_direct(who, dev, kind, op, fmt, rnd, read, d, n, scalar_mask, flags_out, &st))
+            return st;
+    }
     for (int r = 0; r < 3; r++) {
         if (!ptr[r] || !((need >> r) & 1u)) continue;   // unread operands read as +0
         o[r].host = ptr[r];
@@ -636,6 +729,20 @@ static cft_status exec_elem(const char *who, cft_device *dev, int kind, int op, 
         if (!o[r].host || !o[r].buf || !dbuf || o[r].buf != dbuf) continue;
         const bool same = o[r].host == d && !o[r].scalar && !o[r].idx;
         if (!same && windows_overlap(o[r].host, o[r].count * esz, d, n * esz)) copy_aside[r] = true;
+    }
+    for (int r = 0; r < 3; r++)
+        if (o[r].buf && !aligned_for(o[r].host, esz)) copy_aside[r] = true;
+    // An output inside a resident buffer at an offset the kernels cannot
+    // store to is written through the mirror instead: the run's bytes come
+    // home first if the device held newer ones, and the buffer is stale after.
+    cft_buffer *dbuf_mirror = nullptr;
+    if (dbuf && !aligned_for(d, esz)) {
+        if (dbuf->state == B_DIRTY) {
+            cft_status st0 = cft_buffer_from_device(dbuf);
+            if (st0 != CFT_OK) return st0;
+        }
+        dbuf_mirror = dbuf;
+        dbuf = nullptr;
     }
 
     cudaStream_t s0 = dev->s[0];
@@ -778,6 +885,7 @@ static cft_status exec_elem(const char *who, cft_device *dev, int kind, int op, 
     if (e0 != cudaSuccess || e1 != cudaSuccess)
         return poison(dev, who, e0 != cudaSuccess ? e0 : e1);
     if (dbuf) dbuf->state = B_DIRTY;
+    if (dbuf_mirror) dbuf_mirror->state = B_STALE;
     flags_emit(dev, (dev->h_word[0] | dev->h_word[1]) & CFT_FLAGS_ALL, flags_out);
     return CFT_OK;
 }

@@ -49,6 +49,7 @@ struct cft_device {
     int mute = 0;
     int poisoned = 0;
     uint32_t max_scratch = 256;
+    int host_page_tables = 0;     // the GPU walks the host's page tables (ATS)
     cudaStream_t s[2] = {nullptr, nullptr};
     uint32_t *d_word = nullptr;   // device flag/status words, 64 of them
     uint32_t *h_word = nullptr;   // pinned host copy
