@@ -3,6 +3,7 @@ reference itself, run here where its tree is present:
 
     make -C oracle ref                       # the reference library + cft-asm
     python tests/golden/make_programs.py /root/reference
+    python tests/golden/make_programs.py /root/reference odes
 
 For every program source the reference ships (programs/*.cfta and
 certificates/programs/*.cfta) it writes one .npz holding:
@@ -286,5 +287,93 @@ def main(ref):
     print("certificate segments:", len(segs))
 
 
-if __name__ == "__main__":
+if __name__ == "__main__" and len(sys.argv) <= 2:
     main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+
+
+def ode_banks(ref):
+    """The ODE workloads' images and constant banks, with the step sizes the
+    benchmark configurations name: Lorenz-63 RK4 binary256 at h = 0.01 (its
+    classic bank), Lorenz-96 RK4 binary128 at h = 0.005 and Henon-Heiles
+    leapfrog binary256 at h = 0.001, each bank derived as the reference's
+    programs/gen_odes.py:bank_values derives it (h from decimal under RNE,
+    h/2 exact, h/6 one rounding) with the golden model's own arithmetic."""
+    ref = Path(ref)
+    sys.path.insert(0, str(ref / "python"))
+    from cft_golden import chars, formats, softfloat as sf
+
+    def dec(fmt, text):
+        return chars.from_decimal(fmt, text, sf.RND_RNE)[0]
+
+    def bank(kind, fmt, htext):
+        h = dec(fmt, htext)
+        two = dec(fmt, "2")
+        h2, _ = sf.mul(fmt, h, dec(fmt, "0.5"))
+        h6, _ = sf.div(fmt, h, dec(fmt, "6"))
+        if kind == "l63":
+            beta, _ = sf.div(fmt, dec(fmt, "8"), dec(fmt, "3"))
+            vals = [h, h2, h6, two, dec(fmt, "10"), dec(fmt, "28"), beta]
+        elif kind == "l96":
+            vals = [h, h2, h6, two, dec(fmt, "8")]
+        else:
+            mh, _ = sf.neg(fmt, h)
+            vals = [h, h2, mh, dec(fmt, "1"), two]
+        esz = fmt.width // 8
+        return np.frombuffer(b"".join(v.to_bytes(esz, "little") for v in vals), np.uint8)
+
+    l63 = assemble(ref / "programs" / "lorenz63-rk4-fp256.cfta")
+    l63_bank = bank("l63", formats.FP256, "0.01")
+    for kind, name in (("l63", "lorenz63-rk4"), ("l96", "lorenz96-rk4"), ("hh", "henonheiles-lf")):
+        # the derivation reproduces the shipped h = 0.01 banks
+        assert bank(kind, formats.FP256, "0.01").tobytes() == \
+            (ref / "programs" / f"{name}-fp256.classic.bank").read_bytes(), name
+    l96 = (ref / "certificates" / "images" / "lorenz96-rk4-fp128.cftp").read_bytes()
+    hh = assemble(ref / "programs" / "henonheiles-lf-fp256.cfta")
+    np.savez_compressed(OUT.parent / "odes.npz",
+                        l63_image=np.frombuffer(l63, np.uint8), l63_bank=l63_bank,
+                        l96_image=np.frombuffer(l96, np.uint8),
+                        l96_bank=bank("l96", formats.FP128, "0.005"),
+                        hh_image=np.frombuffer(hh, np.uint8),
+                        hh_bank=bank("hh", formats.FP256, "0.001"))
+    print("ode images and banks written")
+
+
+def certificate(ref, name):
+    """Run 0 of certificates/<name>: the image, the classic bank, the lane-major
+    boundary states and each segment's end hash, flags and status - every
+    boundary re-derived here by the reference library from the one before it,
+    so the fixture's bank and image are the ones the certificate ran."""
+    ref = Path(ref)
+    cd = ref / "certificates" / name
+    run0 = (cd / f"{name}.cert").read_text().split("run 1 ")[0]
+    segs = re.findall(r"segment (\d+) start ([0-9a-f]{64}) end ([0-9a-f]{64}) flags (\d+) status (\d+)", run0)
+    lanes = int(re.search(r"^lanes (\d+)$", run0, re.M).group(1))
+    img = (ref / "certificates" / "images" / f"{name}.cftp").read_bytes()
+    assert hashlib.sha256(img).hexdigest() == re.search(r"program-image ([0-9a-f]{64})", run0).group(1)
+    bank = np.frombuffer((ref / "programs" / f"{name}.classic.bank").read_bytes(), np.uint8).copy()
+    tag = b"cft-certificate 1 state\0"
+    h = header(img)
+    W = wl.words(h["prec"])
+    states = [np.frombuffer((cd / "states" / f"run-0-boundary-{i}.bin").read_bytes(), np.uint32)
+              .reshape(-1, W) for i in range(len(segs) + 1)]
+    L = lib()
+    dev = ctypes.c_void_p()
+    assert L.cft_open(None, 0, ctypes.byref(dev)) == 0
+    for i, s in enumerate(segs):
+        assert hashlib.sha256(tag + states[i].tobytes()).hexdigest() == s[1]
+        assert hashlib.sha256(tag + states[i + 1].tobytes()).hexdigest() == s[2]
+        a = np.zeros((lanes, W), np.uint32)
+        out, st = run_ref(L, dev, img, lanes, a, None, None, bank, states[i].copy())
+        assert st == 0 and np.array_equal(out["scratch_out"], states[i + 1]), (name, i)
+        assert out["flags"] == int(s[3]) and out["status"] == int(s[4]), (name, i)
+    np.savez_compressed(OUT.parent / f"{name.split('-')[0]}_cert.npz",
+                        image=np.frombuffer(img, np.uint8), bank=bank, state0=states[0].view(np.uint8),
+                        ends=np.array([s[2] for s in segs]), flags=np.array([int(s[3]) for s in segs]),
+                        status=np.array([int(s[4]) for s in segs]))
+    print(name, "segments:", len(segs), "lanes:", lanes)
+
+
+if __name__ == "__main__" and len(sys.argv) > 2 and sys.argv[2] == "odes":
+    ode_banks(sys.argv[1])
+    certificate(sys.argv[1], "lorenz96-rk4-fp256")
+    certificate(sys.argv[1], "henonheiles-lf-fp256")

@@ -2,7 +2,7 @@
 program the reference ships (tests/golden/programs), with and without a
 lane mask and index tables; the reference's photograph known answer (an
 NVIDIA GPU's recorded deposit hashes for a million-lane camera program);
-and the fp256 Lorenz-63 certificate's segment chain."""
+and the fp256 ODE certificates' segment chains."""
 import ctypes
 import hashlib
 
@@ -67,15 +67,20 @@ def test_photograph_known_answer(gpu):
         assert hashlib.sha256(dep.tobytes()).hexdigest() == want[p], f"pass {p}"
 
 
-def test_lorenz63_certificate_chain(gpu):
-    """Three 100-step segments of the fp256 Lorenz-63 RK4 program from the
-    certificate's boundary-0 state: every boundary's tagged hash, flags and
-    STATUS as the certificate records them."""
-    z = np.load(su.GOLD / "lorenz63_cert.npz")
+CERTS = ["lorenz63", "lorenz96", "henonheiles"]
+
+
+@pytest.mark.parametrize("cert", CERTS)
+def test_certificate_chain(gpu, cert):
+    """The fp256 ODE certificates (Lorenz-63 RK4, Lorenz-96 RK4, Henon-Heiles
+    leapfrog): each segment run from the certificate's boundary state, every
+    boundary's tagged hash, flags and STATUS as the certificate records them."""
+    z = np.load(su.GOLD / f"{cert}_cert.npz")
     img = z["image"].copy()
     bank = z["bank"].copy()
+    slots = su.header(img)["sout"]
     state = z["state0"].copy().view(np.uint32).reshape(-1, 8)
-    n = state.shape[0] // 3
+    n = state.shape[0] // slots
     L = cftgb.lib()
     prog = ctypes.c_void_p()
     cftgb._lib.check(L.cft_program_load(gpu, img.ctypes.data, img.size, ctypes.byref(prog)), "load")

@@ -27,6 +27,29 @@ def test_oracle_executor_matches_reference_outputs(oracle, path):
         assert su.compare(got2, case, "exp2_") == []
 
 
+@pytest.mark.parametrize("cert", ["lorenz63", "lorenz96", "henonheiles"])
+def test_oracle_reproduces_certificates(oracle, cert):
+    """The fp256 ODE certificates' segment chains through the oracle: every
+    boundary's tagged state hash, flags and STATUS as recorded."""
+    import hashlib
+    import oracle_lib
+    z = np.load(su.GOLD / f"{cert}_cert.npz")
+    img, bank = z["image"].copy(), z["bank"].copy()
+    slots = su.header(img)["sout"]
+    state = z["state0"].copy().view(np.uint32).reshape(-1, 8)
+    n = state.shape[0] // slots
+    a = np.zeros((n, 8), np.uint32)
+    for k, end in enumerate(z["ends"]):
+        out = np.zeros_like(state)
+        A = oracle_lib.SeqArgs()
+        A.a, A.n, A.bank = a.ctypes.data, n, bank.ctypes.data
+        A.scratch_in, A.scratch_out, A.depth = state.ctypes.data, out.ctypes.data, 256
+        assert oracle.L.sfp_seq_run(img.ctypes.data, img.size, ctypes.byref(A)) == 0
+        assert hashlib.sha256(b"cft-certificate 1 state\0" + out.tobytes()).hexdigest() == str(end)
+        assert A.flags_out == int(z["flags"][k]) and A.status_out == int(z["status"][k])
+        state = out
+
+
 def test_loader_decisions_match_the_reference():
     z = np.load(su.GOLD / "loader_cases.npz")
     L = cftgb.lib()
