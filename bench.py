@@ -143,6 +143,138 @@ def cpu_baseline(fmt, a, b, c, seconds=12.0, per_call=2048):
     return sum(done) / dt, threads, sum(done), dt
 
 
+ODE_PROGRAMS = (
+    # name, image/bank key, format, state slots, initial value, steps range,
+    # steps a run (the image's REPEAT count), lanes, runs between kept states
+    ("lorenz63-rk4-fp256 h=0.01", "l63", 3, 3, 1.0, (1e3, 1e5), 100, 4096, 10),
+    ("lorenz96-rk4-fp128 N=40 F=8 h=0.005", "l96", 2, 40, 8.0, (1e3, 1e4), 20, 512, 50),
+)
+
+
+def ode_programs(scale=1.0, steps_scale=1.0):
+    """The trajectory workload's programs: images and banks from the
+    committed fixture (the reference's own ODE images; banks for the named
+    step sizes), seeded initial states and uneven run counts. `scale`
+    scales the lane counts and `steps_scale` the step range (both 1 for
+    the configuration; smaller for profiler captures)."""
+    from cftgb import suites
+    z = np.load(ROOT / "tests" / "golden" / "odes.npz")
+    progs = []
+    for i, (name, key, fmt, slots, base, rng, spr, lanes, every) in enumerate(ODE_PROGRAMS):
+        lanes = max(1, int(lanes * scale))
+        rng = (max(spr, rng[0] * steps_scale), max(spr, rng[1] * steps_scale))
+        init, runs = suites.ode_lanes(key, fmt, lanes, slots, base, rng, spr, 1000 + i)
+        progs.append(dict(name=name, image=z[key + "_image"], bank=z[key + "_bank"], fmt=fmt,
+                          slots=slots, init=init, runs=runs, snap_every=every,
+                          max_snaps=int(np.max(runs)) // every + 1, steps_per_run=spr))
+    return progs
+
+
+def traj_oracle_check(progs, res, per_prog=8):
+    """The oracle runs a sample of each program's lanes segment by segment
+    on all host cores: the shortest lanes, lanes at the quartiles and the
+    longest. Every kept state's hash and the final state must equal the
+    GPU's. Returns (mismatches, lanes checked, oracle lane-steps/s, threads,
+    seconds)."""
+    sys.path.insert(0, str(ROOT / "tests"))
+    import hashlib
+    import oracle_lib
+    from cftgb import suites, workload as wl
+    o = oracle_lib.Oracle()
+    jobs = []
+    for P, R in zip(progs, res["programs"]):
+        order = np.argsort(P["runs"], kind="stable")
+        n = len(order)
+        pick = list(order[:per_prog // 2]) + [order[int(q * (n - 1))] for q in (0.25, 0.5, 0.75)]
+        pick.append(order[-1])
+        for lane in dict.fromkeys(int(x) for x in pick):
+            jobs.append((P, R, lane))
+    bad = []
+    steps_done = [0]
+    lock = threading.Lock()
+
+    def one(job):
+        P, R, lane = job
+        W = wl.words(P["fmt"])
+        slots = P["slots"]
+        img = np.ascontiguousarray(P["image"])
+        bank = np.ascontiguousarray(P["bank"])
+        s = np.ascontiguousarray(P["init"][lane * slots:(lane + 1) * slots])
+        a = np.zeros((1, W), np.uint32)
+        hs = R["_hashes"][lane]
+        for k in range(int(P["runs"][lane])):
+            out = np.zeros_like(s)
+            A = oracle_lib.SeqArgs()
+            A.a, A.n, A.bank = a.ctypes.data, 1, bank.ctypes.data
+            A.scratch_in, A.scratch_out, A.depth = s.ctypes.data, out.ctypes.data, 256
+            if o.L.sfp_seq_run(img.ctypes.data, img.size, ctypes.byref(A)) != 0:
+                return (P["name"], lane, "oracle refused")
+            s = out
+            if (k + 1) % P["snap_every"] == 0:
+                j = (k + 1) // P["snap_every"] - 1
+                if j >= len(hs) or hashlib.sha256(suites.TAG + s.tobytes()).digest() != hs[j]:
+                    return (P["name"], lane, f"state hash after run {k + 1}")
+        with lock:
+            steps_done[0] += int(P["runs"][lane]) * P["steps_per_run"]
+        if not np.array_equal(R["_final"][lane * slots:(lane + 1) * slots], s):
+            return (P["name"], lane, "final state")
+        return None
+
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    from concurrent.futures import ThreadPoolExecutor
+    # longest jobs first so the pool's last worker is not the long one
+    jobs.sort(key=lambda j: -int(j[0]["runs"][j[2]]) * j[0]["steps_per_run"] * j[0]["slots"])
+    with ThreadPoolExecutor(threads) as ex:
+        for r in ex.map(one, jobs):
+            if r:
+                bad.append(r)
+    dt = time.perf_counter() - t0
+    return bad, len(jobs), steps_done[0] / dt, min(threads, len(jobs)), dt
+
+
+def run_trajectories(h, suites, args):
+    progs = ode_programs(args.scale, args.steps_scale)
+    res = suites.trajectories(h, progs, reps=2, separate=args.separate)
+    bad, checked, cpu_rate, thr, cpu_s = traj_oracle_check(progs, res)
+    for p in res["programs"]:
+        p.pop("_final")
+        p.pop("_hashes")
+    res["oracle_lanes_checked"] = checked
+    res["oracle_mismatches"] = [list(map(str, b)) for b in bad]
+    res["bit_exact_sample"] = not bad
+    res["cpu_baseline"] = {"value": cpu_rate, "unit": "lane-steps/s", "cores": thr, "kind": "port",
+                           "sample": f"{checked} lanes (shortest, quartiles, longest of each "
+                                     f"program) run whole, {cpu_s:.1f} s"}
+    return res
+
+
+def run_sweep(h, suites, args):
+    """The sweep suite, then the oracle over each cell's checked prefix
+    (values and per-element flag bytes) on all host cores."""
+    sys.path.insert(0, str(ROOT / "tests"))
+    import oracle_lib
+    res = suites.sweep(h, n=min(args.n, 1 << 24))
+    checks = res.pop("_checks")
+    o = oracle_lib.Oracle()
+    from concurrent.futures import ThreadPoolExecutor
+
+    def one(ck):
+        d, lf, _ = o.run(ck["kind"], ck["fmt"], ck["op"], ck["rnd"], ck["a"], ck["b"], ck["c"])
+        vbad = int(np.count_nonzero(np.any(d != ck["d"], axis=1)))
+        fbad = int(np.count_nonzero(lf != ck["lf"]))
+        return vbad, fbad
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(os.cpu_count() or 1) as ex:
+        out = list(ex.map(one, checks))
+    res["oracle_cells_checked"] = len(checks)
+    res["oracle_elements_checked"] = int(sum(len(c["lf"]) for c in checks))
+    res["value_mismatches"] = int(sum(v for v, _ in out))
+    res["flag_mismatches"] = int(sum(f for _, f in out))
+    res["oracle_s"] = time.perf_counter() - t0
+    return res
+
+
 def dist_init():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -197,10 +329,20 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--profile", action="store_true",
                     help="only the device-resident leg (for ncu captures on a small n)")
+    ap.add_argument("--scale", type=float, default=1.0,
+                    help="lane-count scale of the trajectories suite (1.0 = 4,096 + 512 lanes)")
+    ap.add_argument("--steps-scale", type=float, default=1.0,
+                    help="step-range scale of the trajectories suite (1.0 = the configuration)")
+    ap.add_argument("--separate", action="store_true",
+                    help="trajectories suite: also time each program's launch alone")
+    ap.add_argument("--rate", type=float, default=20000.0,
+                    help="offered requests a second of the serving suite")
+    ap.add_argument("--seconds", type=float, default=60.0,
+                    help="length of the serving suite's request stream")
     ap.add_argument("--fmt", type=int, default=3, help="format of the headline leg (3 = binary256)")
     ap.add_argument("--op", default="fma", choices=["fma", "add", "mul", "div", "sqrt"],
                     help="operation of the --profile leg")
-    ap.add_argument("--suite", default=None, choices=["uneven"],
+    ap.add_argument("--suite", default=None, choices=["uneven", "trajectories", "sweep", "serving"],
                     help="run one of the secondary configurations instead of the headline")
     args = ap.parse_args()
     if args.impl == "reference":
@@ -211,7 +353,16 @@ def main():
         from cftgb import suites
         torch.cuda.set_device(0)
         h = cftgb.open_device("cuda:0")
-        print(json.dumps(getattr(suites, args.suite)(h)))
+        if args.suite == "trajectories":
+            print(json.dumps(run_trajectories(h, suites, args)))
+        elif args.suite == "sweep":
+            print(json.dumps(run_sweep(h, suites, args)))
+        elif args.suite == "serving":
+            z = np.load(ROOT / "tests" / "golden" / "odes.npz")
+            print(json.dumps(suites.serving(h, z["hh_image"], z["hh_bank"], rate=args.rate,
+                                            seconds=args.seconds)))
+        else:
+            print(json.dumps(getattr(suites, args.suite)(h)))
         cftgb.close_device(h)
         return
 

@@ -9,8 +9,18 @@ uneven  10,000 independent elementwise calls, sizes log-uniform in
         one persistent work-queue launch replayed from a CUDA graph
         (cftg_batch_*), after the tile autotuner. Outputs of the two are
         compared bit for bit, flags per call included.
+
+trajectories  the batched sequencer: 4,096 Lorenz-63 RK4 lanes at
+        binary256 (h = 0.01, initial state (1,1,1) + N(0, 1e-3) per lane)
+        with step counts log-uniform in [1e3, 1e5], and 512 Lorenz-96 RK4
+        lanes at binary128 (N = 40, F = 8, h = 0.005, initial state
+        8 + N(0, 1e-3)) with step counts log-uniform in [1e3, 1e4], all as ONE
+        CUDA graph launch (cftg_traj_group_*). Every 1,000 steps each lane's
+        state is kept; its tagged SHA-256 and the final states are returned
+        for checking against the oracle run segment by segment.
 """
 import ctypes
+import hashlib
 import time
 
 import numpy as np
@@ -138,3 +148,407 @@ def uneven(h, ncalls=10000, seed=4, max_log2=20, reps=3):
         "tile_lengths": {f"fmt{f}": [int(L.cftg_tile_length(f, k, o)) for k, o in kinds]
                          for f in (1, 2, 3)},
     }
+
+
+TAG = b"cft-certificate 1 state\0"
+
+
+def _bind_traj(L):
+    vp = ctypes.c_void_p
+    L.cftg_traj_create.argtypes = [vp, vp, ctypes.c_size_t, vp, vp, vp, vp, vp, vp,
+                                   ctypes.c_uint32, ctypes.c_uint32, vp, ctypes.POINTER(vp)]
+    L.cftg_traj_result.argtypes = [vp, vp, vp, vp]
+    L.cftg_traj_free.argtypes = [vp]
+    L.cftg_traj_group_capture.argtypes = [ctypes.POINTER(vp), ctypes.c_size_t, vp,
+                                          ctypes.POINTER(vp)]
+    L.cftg_traj_group_launch.argtypes = [vp, vp]
+    L.cftg_traj_group_free.argtypes = [vp]
+    L.cft_program_load.argtypes = [vp, vp, ctypes.c_size_t, ctypes.POINTER(vp)]
+    L.cft_program_free.argtypes = [vp]
+
+
+def ode_lanes(kind, fmt, lanes, slots, base, steps_range, steps_per_run, seed):
+    """Seeded initial blocks (lane-major, `slots` elements a lane: base +
+    N(0, 1e-3) each, rounded to double then widened exactly) and run counts
+    (steps log-uniform in steps_range, rounded to whole runs)."""
+    from . import workload as wl
+    W = wl.words(fmt)
+    rng = np.random.default_rng(seed)
+    vals = base + rng.normal(0.0, 1e-3, size=(lanes, slots))
+    init = np.zeros((lanes * slots, W), np.uint32)
+    for i, v in enumerate(vals.reshape(-1)):
+        init[i] = wl.from_int(wl.encode_double(fmt, float(v)), W)
+    lo, hi = np.log(steps_range[0]), np.log(steps_range[1])
+    steps = np.exp(rng.uniform(lo, hi, size=lanes))
+    runs = np.maximum(1, np.rint(steps / steps_per_run)).astype(np.uint32)
+    return init, runs
+
+
+def state_hashes(snaps, runs, snap_every, max_snaps, slots, W):
+    """Per lane, the tagged SHA-256 of each kept state (one every
+    snap_every runs), and one digest over all of them in lane order."""
+    snaps = snaps.reshape(len(runs), max_snaps, slots * W)
+    per_lane = []
+    outer = hashlib.sha256()
+    for i, r in enumerate(runs):
+        hs = [hashlib.sha256(TAG + snaps[i, k].tobytes()).digest()
+              for k in range(min(max_snaps, int(r) // snap_every))]
+        per_lane.append(hs)
+        for x in hs:
+            outer.update(x)
+    return per_lane, outer.hexdigest()
+
+
+def trajectories(h, progs, reps=2, separate=False):
+    """progs: a list of dicts with image, bank (uint8 arrays), fmt, slots,
+    init (lane-major uint32 blocks), runs (uint32 per lane), snap_every,
+    max_snaps, steps_per_run. Runs them all as one graph launch, `reps`
+    times from the same initial states (the first launch is the warm one),
+    and returns timings plus each program's final states and hashes."""
+    import torch
+    from . import workload as wl
+    L = _lib.lib()
+    _bind_traj(L)
+    vp = ctypes.c_void_p
+    stream = torch.cuda.Stream()
+    keep, handles = [], []
+    for P in progs:
+        W = wl.words(P["fmt"])
+        n = len(P["runs"])
+        prog = vp()
+        img = np.ascontiguousarray(P["image"])
+        _lib.check(L.cft_program_load(h, img.ctypes.data, img.size, ctypes.byref(prog)),
+                   "cft_program_load")
+        t = dict(prog=prog, W=W, n=n)
+        t["a"] = torch.zeros(max(1, n) * W, dtype=torch.int32, device="cuda")
+        t["bank"] = torch.from_numpy(np.ascontiguousarray(P["bank"]).view(np.int32).copy()).cuda()
+        t["init"] = torch.from_numpy(np.ascontiguousarray(P["init"]).view(np.int32).copy()).cuda()
+        t["state"] = t["init"].clone()
+        t["snaps"] = torch.zeros(n * P["max_snaps"] * P["slots"] * W, dtype=torch.int32,
+                                 device="cuda")
+        t["lf"] = torch.zeros(max(1, n), dtype=torch.uint8, device="cuda")
+        runs = np.ascontiguousarray(P["runs"], np.uint32)
+        tr = vp()
+        _lib.check(L.cftg_traj_create(prog, runs.ctypes.data, n, t["a"].data_ptr(), None, None,
+                                      t["bank"].data_ptr(), t["state"].data_ptr(),
+                                      t["snaps"].data_ptr(), P["snap_every"], P["max_snaps"],
+                                      t["lf"].data_ptr(), ctypes.byref(tr)), "cftg_traj_create")
+        t["traj"] = tr
+        keep.append(t)
+        handles.append(tr)
+    arr = (vp * len(handles))(*[x.value for x in handles])
+    group = vp()
+    _lib.check(L.cftg_traj_group_capture(arr, len(handles), stream.cuda_stream, ctypes.byref(group)),
+               "cftg_traj_group_capture")
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    times = []
+    for _ in range(reps):
+        for t in keep:
+            t["state"].copy_(t["init"])
+            t["snaps"].zero_()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        _lib.check(L.cftg_traj_group_launch(group, stream.cuda_stream), "cftg_traj_group_launch")
+        e1.record(stream)
+        stream.synchronize()
+        times.append(e0.elapsed_time(e1) / 1e3)
+    out = {"suite": "trajectories", "launch_s": min(times), "launches": reps, "programs": []}
+    if separate:
+        # each program's launch alone, for the breakdown
+        L.cftg_traj_launch.argtypes = [vp, vp]
+        for P, t in zip(progs, keep):
+            t["state"].copy_(t["init"])
+            torch.cuda.synchronize()
+            e0.record(stream)
+            _lib.check(L.cftg_traj_launch(t["traj"], stream.cuda_stream), "cftg_traj_launch")
+            e1.record(stream)
+            stream.synchronize()
+            t["alone_s"] = e0.elapsed_time(e1) / 1e3
+        for t in keep:                  # the reported states are the group launch's
+            t["state"].copy_(t["init"])
+        _lib.check(L.cftg_traj_group_launch(group, stream.cuda_stream), "cftg_traj_group_launch")
+        stream.synchronize()
+    total_steps = 0
+    for P, t in zip(progs, keep):
+        fl, st = ctypes.c_uint32(), ctypes.c_uint32()
+        _lib.check(L.cftg_traj_result(t["traj"], ctypes.byref(fl), ctypes.byref(st),
+                                      stream.cuda_stream), "cftg_traj_result")
+        W = t["W"]
+        final = t["state"].cpu().numpy().view(np.uint32).reshape(-1, W)
+        snaps = t["snaps"].cpu().numpy().view(np.uint32)
+        per_lane, digest = state_hashes(snaps, P["runs"], P["snap_every"], P["max_snaps"],
+                                        P["slots"], W)
+        steps = int(np.sum(P["runs"], dtype=np.int64)) * P["steps_per_run"]
+        total_steps += steps
+        out["programs"].append({
+            "name": P.get("name", "?"), "lanes": t["n"], "lane_steps": steps,
+            "alone_s": t.get("alone_s"),
+            "max_steps": int(np.max(P["runs"])) * P["steps_per_run"],
+            "flags": fl.value, "status": st.value, "state_hash_digest": digest,
+            "final_digest": hashlib.sha256(TAG + final.tobytes()).hexdigest(),
+            "_final": final, "_hashes": per_lane})
+    L.cftg_traj_group_free(group)
+    for t in keep:
+        L.cftg_traj_free(t["traj"])
+        L.cft_program_free(t["prog"])
+    out["lane_steps"] = total_steps
+    out["lane_steps_per_s"] = total_steps / out["launch_s"]
+    return out
+
+
+SWEEP_OPS = (("add", 0, 1), ("sub", 0, 2), ("mul", 0, 3), ("fma", 0, 0), ("div", 1, 0),
+             ("sqrt", 2, 0))
+
+
+def sweep(h, n=1 << 24, reps=3, check_n=4096, seed=11):
+    """The elementwise sweep: every format x {add, sub, mul, fma, div, sqrt}
+    x rounding attribute over n device-generated operands a cell (the
+    benchmark's value mix). Each cell is timed over `reps` launches with CUDA
+    events; a prefix of check_n elements is run once more with per-element
+    flag bytes and returned (operands, results, flags) for the oracle."""
+    import torch
+    from . import workload as wl
+    L = _lib.lib()
+    _bind(L)
+    stream = torch.cuda.current_stream()
+    s = stream.cuda_stream
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    word = torch.zeros(1, dtype=torch.int32, device="cuda")
+    cells, checks = [], []
+    for fmt in range(4):
+        W = wl.words(fmt)
+        ops = [torch.empty(n * W, dtype=torch.int32, device="cuda") for _ in range(4)]
+        for j in range(3):
+            _lib.check(L.cftg_fill_operands(fmt, ops[j].data_ptr(), n, seed * 16 + fmt * 4 + j, 64,
+                                            100000, s), "cftg_fill_operands")
+        lf = torch.zeros(check_n, dtype=torch.uint8, device="cuda")
+        pa, pb, pc, pd = (x.data_ptr() for x in ops)
+        for name, kind, op in SWEEP_OPS:
+            for rnd in range(5):
+                def go(nn, lfp):
+                    st = L.cftg_run_device(h, kind, op, fmt, rnd, pa, pb, pc, pd, nn, 0, lfp,
+                                           word.data_ptr(), s)
+                    _lib.check(st, "cftg_run_device")
+                go(n, None)
+                torch.cuda.synchronize()
+                e0.record(stream)
+                for _ in range(reps):
+                    go(n, None)
+                e1.record(stream)
+                torch.cuda.synchronize()
+                ms = e0.elapsed_time(e1) / reps
+                cells.append({"fmt": ("fp32", "fp64", "fp128", "fp256")[fmt], "op": name,
+                              "rnd": rnd, "ms": ms, "gelem_s": n / ms / 1e6})
+                go(check_n, lf.data_ptr())
+                torch.cuda.synchronize()
+                host = [x[:check_n * W].cpu().numpy().view(np.uint32).reshape(-1, W) for x in ops]
+                checks.append(dict(fmt=fmt, kind=kind, op=op, rnd=rnd, a=host[0], b=host[1],
+                                   c=host[2], d=host[3], lf=lf.cpu().numpy().copy()))
+        del ops
+    return {"suite": "sweep", "elements_per_cell": n, "cells": cells, "_checks": checks}
+
+
+def hh_init(lanes, seed):
+    """Henon-Heiles initial blocks (x, y, px, py) at energy 1/8, lane-major
+    binary256: x = 0, y and py drawn, px from the energy in double, each
+    value widened exactly."""
+    from . import workload as wl
+    rng = np.random.default_rng(seed)
+    out = np.zeros((lanes * 4, 8), np.uint32)
+    for i in range(lanes):
+        while True:
+            y = rng.uniform(-0.3, 0.4)
+            py = rng.uniform(-0.3, 0.3)
+            rest = 2 * (0.125 - (y * y / 2 - y ** 3 / 3)) - py * py
+            if rest > 0:
+                break
+        for j, v in enumerate((0.0, y, float(np.sqrt(rest)), py)):
+            out[i * 4 + j] = wl.from_int(wl.encode_double(3, v), 8)
+    return out
+
+
+def serving(h, hh_image, hh_bank, rate=20000.0, seconds=60.0, seed=5, budget=40 << 30,
+            program_frac=0.02, hh_lanes=32, max_log2=22, sample_every=2000, max_inflight=6,
+            max_program_inflight=6):
+    """Open-loop serving: requests arrive as a Poisson stream of `rate` a
+    second for `seconds`; each is an element call (binary128 or binary256
+    1:1, size log-uniform in [64, 2^max_log2], operation uniform over add,
+    sub, mul, fma, div, sqrt, rounding attribute uniform) over operands
+    resident in HBM, or (a fraction program_frac) a Henon-Heiles leapfrog
+    ensemble of hh_lanes lanes at binary256 (h = 1e-3, energy 1/8) for
+    1e3..1e4 steps (log-uniform). The server admits them by a budget of
+    `budget` bytes. Latency is completion time minus scheduled arrival.
+    Every sample_every-th request keeps its output for the comparison with
+    the same request run alone."""
+    import torch
+    from . import serving as sv
+    from . import workload as wl
+    L = _lib.lib()
+    _bind(L)
+    sv._bind(L)
+    stream = torch.cuda.current_stream().cuda_stream
+    rng = np.random.default_rng(seed)
+    maxn = 1 << max_log2
+    POOL = 1 << 23
+    pools = {}
+    for fmt in (2, 3):
+        W = wl.words(fmt)
+        pools[fmt] = [torch.empty((POOL + maxn) * W, dtype=torch.int32, device="cuda")
+                      for _ in range(3)]
+        for j in range(3):
+            _lib.check(L.cftg_fill_operands(fmt, pools[fmt][j].data_ptr(), POOL + maxn,
+                                            seed * 10 + fmt * 3 + j, 64, 100000, stream), "fill")
+    prog = ctypes.c_void_p()
+    img = np.ascontiguousarray(hh_image)
+    _lib.check(L.cft_program_load(h, img.ctypes.data, img.size, ctypes.byref(prog)), "load")
+    bank = torch.from_numpy(np.ascontiguousarray(hh_bank).view(np.int32).copy()).cuda()
+    inits = [hh_init(hh_lanes, 7000 + k) for k in range(16)]
+    torch.cuda.synchronize()
+
+    count = int(rate * seconds * 1.05) + 16
+    gaps = rng.exponential(1.0 / rate, size=count)
+    arrive = np.cumsum(gaps)
+    count = int(np.searchsorted(arrive, seconds))
+    arrive = arrive[:count]
+    is_prog = rng.random(count) < program_frac
+    fmts = rng.choice([2, 3], size=count)
+    sizes = np.exp(rng.uniform(np.log(64), np.log(maxn), size=count)).astype(np.int64)
+    opsel = rng.integers(0, 6, size=count)
+    rnds = rng.integers(0, 5, size=count)
+    offs = rng.integers(0, POOL, size=count)
+    steps = np.exp(rng.uniform(np.log(1e3), np.log(1e4), size=count))
+    runs = np.maximum(10, np.rint(steps / 100)).astype(np.int64)   # the image runs 100 steps
+    which_init = rng.integers(0, 16, size=count)
+    OPS = SWEEP_OPS
+    base = {f: [x.data_ptr() for x in pools[f]] for f in (2, 3)}
+    samples = {}
+    req = sv.Request()
+    comp = []
+    with sv.Server(h, budget, max_inflight=max_inflight, max_program_inflight=max_program_inflight,
+                   max_batch_calls=4096, max_batch_lanes=1 << 16) as srv:
+        t0 = sv.clock_ns() + 20_000_000
+        arr_ns = (t0 + arrive * 1e9).astype(np.int64)
+        i = loops = 0
+        while i < count:
+            now = sv.clock_ns()
+            while i < count and arr_ns[i] <= now:
+                sample = (i % sample_every) == 0
+                req.tag = i
+                req.t_arrival_ns = int(arr_ns[i])
+                req.host_out = None
+                if is_prog[i]:
+                    req.type = sv.REQ_PROGRAM
+                    req.prog = prog
+                    req.d_bank = bank.data_ptr()
+                    init = inits[int(which_init[i])]
+                    req.init = init.ctypes.data
+                    req.lanes = hh_lanes
+                    req.runs = int(runs[i])
+                    req.n = 0
+                    if sample:
+                        out = torch.empty(init.nbytes, dtype=torch.uint8, pin_memory=True)
+                        req.host_out = out.data_ptr()
+                        samples[i] = ("prog", int(which_init[i]), int(runs[i]), out)
+                else:
+                    f = int(fmts[i])
+                    esz = 4 * wl.words(f)
+                    n = int(sizes[i])
+                    _, kind, op = OPS[int(opsel[i])]
+                    o = int(offs[i]) * esz
+                    req.type = sv.REQ_ELEM
+                    req.kind, req.op, req.fmt, req.rnd = kind, op, f, int(rnds[i])
+                    req.d_a, req.d_b, req.d_c = base[f][0] + o, base[f][1] + o, base[f][2] + o
+                    req.n = n
+                    req.prog = None
+                    if sample:
+                        out = torch.empty(n * esz, dtype=torch.uint8, pin_memory=True)
+                        req.host_out = out.data_ptr()
+                        samples[i] = ("elem", kind, op, f, int(rnds[i]), req.d_a, req.d_b, req.d_c,
+                                      n, out)
+                st = srv.submit(req)
+                if st:
+                    raise RuntimeError(f"submit refused request {i}: status {st}")
+                i += 1
+            loops += 1
+            if loops % 64 == 0:
+                comp.append(srv.poll())
+            time.sleep(0.0002)
+        t_sub_end = sv.clock_ns()
+        _lib.check(srv.drain(), "cftg_server_drain")
+        t_end = sv.clock_ns()
+        comp.append(srv.poll())
+        stats = srv.stats()
+    done = np.concatenate(comp)
+    lat = (done["t_done_ns"].astype(np.int64) - done["t_arrival_ns"].astype(np.int64)) / 1e6
+    tags = done["tag"].astype(np.int64)
+    prog_mask = is_prog[tags]
+
+    def pct(x):
+        return {"p50_ms": float(np.percentile(x, 50)), "p99_ms": float(np.percentile(x, 99)),
+                "p999_ms": float(np.percentile(x, 99.9)), "max_ms": float(np.max(x))} if len(x) else {}
+    wall = (t_end - t0) / 1e9
+    elem_done = int(sizes[tags[~prog_mask]].sum())
+    lane_steps = int((runs[tags[prog_mask]] * 100 * hh_lanes).sum())
+    # each sampled request again, alone
+    word = torch.zeros(1, dtype=torch.int32, device="cuda")
+    flags = {int(t): int(f) for t, f in zip(done["tag"], done["flags"])}
+    bad = []
+    for tag, m in samples.items():
+        if m[0] == "elem":
+            _, kind, op, f, rnd, pa, pb, pc, n, out = m
+            d = torch.empty(n * 4 * wl.words(f), dtype=torch.uint8, device="cuda")
+            word.zero_()
+            _lib.check(L.cftg_run_device(h, kind, op, f, rnd, pa, pb, pc, d.data_ptr(), n, 0, None,
+                                         word.data_ptr(), stream), "cftg_run_device")
+            torch.cuda.synchronize()
+            if not torch.equal(d.cpu(), out) or flags[tag] != (int(word.item()) & 0x1F):
+                bad.append({"tag": tag, "n": n, "fmt": f, "kind": kind, "op": op,
+                            "bits_equal": bool(torch.equal(d.cpu(), out)),
+                            "flags_mix": flags[tag], "flags_alone": int(word.item()) & 0x1F})
+        else:
+            _, k, r, out = m
+            final, fl = _traj_alone(L, prog, bank, inits[k], hh_lanes, r)
+            mix = out.numpy().view(np.uint32).reshape(hh_lanes, -1)
+            alone = final.reshape(hh_lanes, -1)
+            lanes_off = [j for j in range(hh_lanes) if not np.array_equal(mix[j], alone[j])]
+            if lanes_off or flags[tag] != fl:
+                bad.append({"tag": tag, "runs": r, "lanes_differ": lanes_off[:8],
+                            "n_lanes_differ": len(lanes_off), "flags_mix": flags[tag],
+                            "flags_alone": fl, "zero_lanes_mix": int((~mix.any(axis=1)).sum())})
+    L.cft_program_free(prog)
+    return {
+        "suite": "serving", "offered_req_s": rate, "seconds": seconds, "requests": int(count),
+        "program_requests": int(is_prog.sum()), "completed": int(len(done)),
+        "failed": int((done["result"] != 0).sum()),
+        "wall_s": wall, "submit_lag_s": (t_sub_end - t0) / 1e9 - float(arrive[-1]),
+        "served_gelem_s": elem_done / wall / 1e9, "elements": elem_done,
+        "program_lane_steps_per_s": lane_steps / wall,
+        "latency_all": pct(lat), "latency_elem": pct(lat[~prog_mask]),
+        "latency_program": pct(lat[prog_mask]),
+        "batches": int(stats["batches"]), "bytes_peak": int(stats["bytes_peak"]),
+        "budget": int(budget), "samples_checked": len(samples), "sample_mismatches": bad,
+        "bit_exact_alone_vs_mix": not bad,
+        "mix": {"formats": "fp128:fp256 1:1", "sizes": f"log-uniform [64, 2^{max_log2}]",
+                "ops": "add/sub/mul/fma/div/sqrt uniform", "program_frac": program_frac,
+                "program": f"henonheiles-lf-fp256 h=1e-3 E=1/8, {hh_lanes} lanes, 1e3..1e4 steps"},
+    }
+
+
+def _traj_alone(L, prog, bank, init, lanes, runs):
+    import torch
+    _bind_traj(L)
+    L.cftg_traj_launch.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+    ts = torch.from_numpy(init.view(np.int32).copy()).cuda()
+    ta = torch.zeros(lanes * 8, dtype=torch.int32, device="cuda")
+    lf = torch.zeros(lanes, dtype=torch.uint8, device="cuda")
+    segs = np.full(lanes, runs, np.uint32)
+    t = ctypes.c_void_p()
+    _lib.check(L.cftg_traj_create(prog, segs.ctypes.data, lanes, ta.data_ptr(), None, None,
+                                  bank.data_ptr(), ts.data_ptr(), None, 0, 0, lf.data_ptr(),
+                                  ctypes.byref(t)), "cftg_traj_create")
+    s = torch.cuda.current_stream().cuda_stream
+    _lib.check(L.cftg_traj_launch(t, s), "cftg_traj_launch")
+    fl, st = ctypes.c_uint32(), ctypes.c_uint32()
+    _lib.check(L.cftg_traj_result(t, ctypes.byref(fl), ctypes.byref(st), s), "cftg_traj_result")
+    L.cftg_traj_free(t)
+    return ts.cpu().numpy().view(np.uint32), int(np.bitwise_or.reduce(lf.cpu().numpy() & 0x1F))

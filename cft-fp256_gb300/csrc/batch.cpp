@@ -45,6 +45,15 @@ void tile_defaults()
 
 }  // namespace
 
+namespace cftg {
+double queue_cost(int fmt, int kind) { return cost(fmt, kind); }
+uint32_t queue_tile(int fmt, int kind)
+{
+    tile_defaults();
+    return g_tile[fmt][kind];
+}
+}  // namespace cftg
+
 struct cftg_batch {
     cft_device *dev = nullptr;
     QCall *d_calls = nullptr;

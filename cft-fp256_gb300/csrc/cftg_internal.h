@@ -85,6 +85,7 @@ struct TrajLaunch {
     uint32_t snap_every = 0, max_snaps = 0;
     void *scratch = nullptr;      // n * reach * esz
     uint8_t *lane_flags = nullptr;
+    uint32_t *lane_status = nullptr;   // n words: each lane's STATUS, or NULL
     uint32_t *word = nullptr;     // [0] flags, [1] status, [2] error
 };
 

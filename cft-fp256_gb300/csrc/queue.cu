@@ -124,6 +124,54 @@ __global__ void __launch_bounds__(256) k_queue(const QCall *__restrict__ calls,
     }
 }
 
+__global__ void __launch_bounds__(256) k_queue_calls(const QCall *__restrict__ calls,
+                                                     const uint32_t *__restrict__ prefix,
+                                                     uint32_t ncalls, uint32_t *counter,
+                                                     uint32_t *call_flags)
+{
+    __shared__ uint32_t next, which;
+    const uint32_t total = prefix[ncalls];
+    for (;;) {
+        if (threadIdx.x == 0) {
+            const uint32_t t = atomicAdd(counter, 1u);
+            uint32_t lo = 0, hi = ncalls - 1;        // the last call with prefix <= t
+            if (t < total) {
+                while (lo < hi) {
+                    const uint32_t mid = (lo + hi + 1) >> 1;
+                    if (prefix[mid] <= t) lo = mid;
+                    else hi = mid - 1;
+                }
+            }
+            next = t;
+            which = lo;
+        }
+        __syncthreads();
+        const uint32_t t = next, ci = which;
+        __syncthreads();
+        if (t >= total) break;
+        const QCall c = calls[ci];
+        const uint64_t start = (uint64_t)(t - prefix[ci]) * c.tile;
+        const uint32_t len = (uint32_t)(c.n - start < c.tile ? c.n - start : c.tile);
+        uint32_t acc;
+        switch (c.fmt) {
+        case 0: acc = tile_fmt<0>(c, start, len); break;
+        case 1: acc = tile_fmt<1>(c, start, len); break;
+        case 2: acc = tile_fmt<2>(c, start, len); break;
+        default: acc = tile_fmt<3>(c, start, len); break;
+        }
+        acc = __reduce_or_sync(0xFFFFFFFFu, acc);
+        if ((threadIdx.x & 31) == 0 && acc) atomicOr(call_flags + ci, acc);
+    }
+}
+
+cudaError_t launch_queue_calls(const QCall *calls, const uint32_t *prefix, uint32_t ncalls,
+                               uint32_t *counter, uint32_t *call_flags, int blocks, cudaStream_t s)
+{
+    if (ncalls == 0) return cudaSuccess;
+    k_queue_calls<<<blocks, 256, 0, s>>>(calls, prefix, ncalls, counter, call_flags);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_queue(const QCall *calls, const QTile *tiles, uint32_t ntiles, uint32_t *counter,
                          uint32_t *call_flags, int blocks, cudaStream_t s)
 {

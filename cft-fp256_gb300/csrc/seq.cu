@@ -122,8 +122,11 @@ struct LaneRun {
 
 // One run of the program for this lane (reference seq_exec.h:412-685):
 // control decided per warp, arithmetic per active lane. `active` starts as
-// the lane's keep bit; `dep` is the deposit buffer (AoS) or NULL.
-template <int FMT>
+// the lane's keep bit; `dep` is the deposit buffer (AoS) or NULL. UNIFIED
+// runs FMA/ADD/SUB/MUL through one FMA code path (arith_rt): more work for
+// ADD and MUL, a quarter of the code, which is what a launch of few, long
+// lanes (latency-bound, one warp a scheduler) wants.
+template <int FMT, bool UNIFIED = false>
 SFD void interpret(const SeqProgram &P, const Lane<sf::Fmt<FMT>::W> &R,
                    const Scratch<sf::Fmt<FMT>::W> &sc, uint32_t *dep, size_t lane, bool keep,
                    bool active, LaneRun &o)
@@ -148,12 +151,16 @@ SFD void interpret(const SeqProgram &P, const Lane<sf::Fmt<FMT>::W> &R,
                 if (ka) { for (int w = 0; w < W; w++) va[w] = __ldg(kons + ia * W + w); } else R.get(ia, va);
                 if (kb) { for (int w = 0; w < W; w++) vb[w] = __ldg(kons + ib * W + w); } else R.get(ib, vb);
                 if (kc) { for (int w = 0; w < W; w++) vc[w] = __ldg(kons + ic * W + w); } else R.get(ic, vc);
-                switch (d.op) {
-                case 0: sf::arith<FMT, sf::OP_FMA>(va, vb, vc, d.rnd, o, fl); break;
-                case 1: sf::arith<FMT, sf::OP_ADD>(va, vb, vc, d.rnd, o, fl); break;
-                case 2: sf::arith<FMT, sf::OP_SUB>(va, vb, vc, d.rnd, o, fl); break;
-                case 3: sf::arith<FMT, sf::OP_MUL>(va, vb, vc, d.rnd, o, fl); break;
-                default: sf::simple<FMT>(d.op, va, vb, vc, o, fl); break;
+                if (UNIFIED && d.op <= 3) {
+                    sf::arith_rt<FMT>(d.op, va, vb, vc, d.rnd, o, fl);
+                } else {
+                    switch (d.op) {
+                    case 0: sf::arith<FMT, sf::OP_FMA>(va, vb, vc, d.rnd, o, fl); break;
+                    case 1: sf::arith<FMT, sf::OP_ADD>(va, vb, vc, d.rnd, o, fl); break;
+                    case 2: sf::arith<FMT, sf::OP_SUB>(va, vb, vc, d.rnd, o, fl); break;
+                    case 3: sf::arith<FMT, sf::OP_MUL>(va, vb, vc, d.rnd, o, fl); break;
+                    default: sf::simple<FMT>(d.op, va, vb, vc, o, fl); break;
+                    }
                 }
                 R.put(reg5(d.rd, d.imm, 0), o);
                 if (!qd) {
@@ -405,9 +412,10 @@ __global__ void k_seq(const SeqLaunch L, size_t lane0, size_t nl)
 // sorts them by segment count, longest first, so a warp's lanes finish
 // together); a lane whose segments are done is inactive for the rest of its
 // warp's runs. Every `snap_every` runs the carried block is copied to the
-// lane's snapshot list. Flags, STATUS and the lane byte are ORed over runs.
+// lane's snapshot list. Flags, STATUS and the lane byte are ORed over runs
+// (STATUS also per lane when lane_status is given). A NULL a stream reads +0.
 template <int FMT>
-__global__ void k_traj(const TrajLaunch L)
+__global__ void k_traj(const TrajLaunch L, bool scratch_shared)
 {
     constexpr int W = sf::Fmt<FMT>::W;
     extern __shared__ uint32_t smem[];
@@ -420,7 +428,11 @@ __global__ void k_traj(const TrajLaunch L)
     const int nregs = (int)P.nregs;
     const uint32_t slots = P.n_scratch_out;
     Lane<W> R{smem, T, t};
-    const Scratch<W> sc{static_cast<uint32_t *>(L.scratch), L.n, local};
+    // the scratch block in shared memory behind the registers when it fits
+    // (a trajectory's state lives there for the whole launch), else global
+    const Scratch<W> sc = scratch_shared
+        ? Scratch<W>{smem + (size_t)(nregs > 0 ? nregs : 1) * W * T, (size_t)T, (size_t)t}
+        : Scratch<W>{static_cast<uint32_t *>(L.scratch), L.n, local};
     uint32_t *state = static_cast<uint32_t *>(L.state);
     uint32_t *snaps = static_cast<uint32_t *>(L.snaps);
     uint32_t x[W];
@@ -440,7 +452,7 @@ __global__ void k_traj(const TrajLaunch L)
             for (int w = 0; w < W; w++) R.at(r, w) = 0u;
         }
         if (mine) {
-            if (nregs > 0) { load_in<W>(L.a, nullptr, lane, x); R.put(0, x); }
+            if (nregs > 0 && L.a) { load_in<W>(L.a, nullptr, lane, x); R.put(0, x); }
             if (nregs > 1 && L.b) { load_in<W>(L.b, nullptr, lane, x); R.put(1, x); }
             if (nregs > 2 && L.c) { load_in<W>(L.c, nullptr, lane, x); R.put(2, x); }
             if (sc.base) {
@@ -452,7 +464,7 @@ __global__ void k_traj(const TrajLaunch L)
         }
         __syncwarp();
         LaneRun o;
-        interpret<FMT>(P, R, sc, nullptr, lane, mine, mine, o);
+        interpret<FMT, true>(P, R, sc, nullptr, lane, mine, mine, o);
         flags |= o.flags;
         status |= o.status;
         err |= o.err;
@@ -476,6 +488,7 @@ __global__ void k_traj(const TrajLaunch L)
             }
         }
         if (L.lane_flags) L.lane_flags[lane] = lflag;
+        if (L.lane_status) L.lane_status[lane] = status;
     }
     flags = __reduce_or_sync(0xFFFFFFFFu, flags);
     status = __reduce_or_sync(0xFFFFFFFFu, status);
@@ -501,16 +514,30 @@ static int seq_threads(const SeqProgram &P, size_t *smem)
     return T;
 }
 
+// A trajectory launch usually holds few lanes (thousands), each running
+// long: blocks are made just large enough that the lanes spread over every
+// SM, so that each warp has a scheduler to itself as far as there are SMs.
 template <int FMT>
 static cudaError_t go_traj(const TrajLaunch &L, cudaStream_t s)
 {
+    constexpr int W = sf::Fmt<FMT>::W;
     size_t smem = 0;
-    const int T = seq_threads<FMT>(L.P, &smem);
+    int T = seq_threads<FMT>(L.P, &smem);
+    const size_t sms = (size_t)sm_count();
+    const size_t spread = ((L.n + sms - 1) / sms + 31) / 32 * 32;
+    const size_t regs = (size_t)(L.P.nregs > 0 ? L.P.nregs : 1) * W * 4;
+    if (spread < (size_t)T) {
+        T = (int)spread;
+        smem = regs * T;
+    }
+    const size_t scr = (size_t)L.P.reach * W * 4;
+    const bool shared = L.P.reach > 0 && (regs + scr) * T <= (160u << 10);
+    if (shared) smem += scr * T;
     cudaError_t e = cudaFuncSetAttribute(k_traj<FMT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     if (e != cudaSuccess) return e;
     const size_t blocks = (L.n + T - 1) / T;
-    k_traj<FMT><<<(unsigned)blocks, T, smem, s>>>(L);
+    k_traj<FMT><<<(unsigned)blocks, T, smem, s>>>(L, shared);
     return cudaGetLastError();
 }
 

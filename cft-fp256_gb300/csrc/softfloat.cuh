@@ -422,6 +422,34 @@ SFD void arith(const uint32_t (&x)[Fmt<FMT>::W], const uint32_t (&y)[Fmt<FMT>::W
     fma_general<FMT, OP>(ua, ub, uc, uc.sign, rnd, out, flags);
 }
 
+// FMA/ADD/SUB/MUL with the operation chosen at run time, all through the one
+// FMA code path: ADD/SUB steer b to +1 (a*1 is exact) and SUB flips c's sign,
+// MUL steers c to a zero of the product's sign, exactly the reference's
+// steering; the special cases then see the steered operands. One copy of
+// the code serves every arithmetic opcode, which keeps an interpreter's
+// instruction footprint small and lets threads that run different opcodes
+// of this family stay converged.
+template <int FMT>
+SFD void arith_rt(int op, const uint32_t (&x)[Fmt<FMT>::W], const uint32_t (&y)[Fmt<FMT>::W],
+                  const uint32_t (&z)[Fmt<FMT>::W], int rnd, uint32_t (&out)[Fmt<FMT>::W],
+                  uint32_t &flags)
+{
+    using F = Fmt<FMT>;
+    constexpr int W = F::W;
+    constexpr int ES = exp_shift<FMT>();
+    const bool addsub = op == OP_ADD || op == OP_SUB;
+    uint32_t b[W], c[W];
+#pragma unroll
+    for (int i = 0; i < W; i++) {
+        b[i] = addsub ? 0u : y[i];
+        c[i] = op == OP_MUL ? 0u : z[i];
+    }
+    if (addsub) b[W - 1] = (uint32_t)F::BIAS << ES;                       // +1
+    if (op == OP_SUB) c[W - 1] ^= 0x80000000u;
+    if (op == OP_MUL) c[W - 1] = (x[W - 1] ^ y[W - 1]) & 0x80000000u;    // +-0
+    arith<FMT, OP_FMA>(x, b, c, rnd, out, flags);
+}
+
 // ---- exact division of significands ---------------------------------------
 
 // q (W+1 words) = floor(X * 2^(32W) / Y) and rnz = (remainder != 0), for X, Y

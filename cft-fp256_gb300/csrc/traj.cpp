@@ -181,3 +181,87 @@ extern "C" cft_status cftg_traj_result(cftg_traj *t, uint32_t *flags_out, uint32
     if (status_out) *status_out = w[1];
     return CFT_OK;
 }
+
+// Several trajectory runs (of different programs and formats) recorded as
+// one CUDA graph: every run an independent branch, so one graph launch puts
+// them all on the device at once and they share the SMs.
+struct cftg_traj_group {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+};
+
+extern "C" void cftg_traj_group_free(cftg_traj_group *g)
+{
+    if (!g) return;
+    if (g->exec) cudaGraphExecDestroy(g->exec);
+    if (g->graph) cudaGraphDestroy(g->graph);
+    delete g;
+}
+
+extern "C" cft_status cftg_traj_group_capture(cftg_traj *const *runs, size_t count, void *stream,
+                                              cftg_traj_group **out)
+{
+    clear_error();
+    if (!out || !runs || !count || !stream) {
+        set_error("cftg_traj_group_capture: needs runs, a count, a stream other than the legacy "
+                  "default and out");
+        return CFT_ERR_INVALID_ARGUMENT;
+    }
+    *out = nullptr;
+    for (size_t i = 0; i < count; i++)
+        if (!runs[i] || runs[i]->dev != runs[0]->dev) {
+            set_error("cftg_traj_group_capture: run %zu is NULL or on another device", i);
+            return CFT_ERR_INVALID_ARGUMENT;
+        }
+    cftg_traj_group *g = new (std::nothrow) cftg_traj_group();
+    if (!g) return CFT_ERR_OUT_OF_MEMORY;
+    cudaStream_t s = (cudaStream_t)stream;
+    std::vector<cudaStream_t> side(count, nullptr);
+    std::vector<cudaEvent_t> join(count, nullptr);
+    cudaEvent_t fork = nullptr;
+    cudaError_t e = cudaEventCreateWithFlags(&fork, cudaEventDisableTiming);
+    for (size_t i = 1; e == cudaSuccess && i < count; i++) {
+        e = cudaStreamCreateWithFlags(&side[i], cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&join[i], cudaEventDisableTiming);
+    }
+    if (e == cudaSuccess) e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        cudaError_t e2 = cudaEventRecord(fork, s);
+        for (size_t i = 1; e2 == cudaSuccess && i < count; i++) {
+            e2 = cudaStreamWaitEvent(side[i], fork, 0);
+            if (e2 == cudaSuccess) e2 = traj_enqueue(runs[i], side[i]);
+            if (e2 == cudaSuccess) e2 = cudaEventRecord(join[i], side[i]);
+            if (e2 == cudaSuccess) e2 = cudaStreamWaitEvent(s, join[i], 0);
+        }
+        if (e2 == cudaSuccess) e2 = traj_enqueue(runs[0], s);
+        e = cudaStreamEndCapture(s, &g->graph);
+        if (e2 != cudaSuccess) e = e2;
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&g->exec, g->graph, 0);
+    for (size_t i = 1; i < count; i++) {
+        if (join[i]) cudaEventDestroy(join[i]);
+        if (side[i]) cudaStreamDestroy(side[i]);
+    }
+    if (fork) cudaEventDestroy(fork);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        cftg_traj_group_free(g);
+        set_error("cftg_traj_group_capture: %s", cudaGetErrorString(e));
+        return CFT_ERR_INTERNAL;
+    }
+    *out = g;
+    return CFT_OK;
+}
+
+extern "C" cft_status cftg_traj_group_launch(cftg_traj_group *g, void *stream)
+{
+    clear_error();
+    if (!g || !g->exec) return CFT_ERR_INVALID_ARGUMENT;
+    cudaError_t e = cudaGraphLaunch(g->exec, (cudaStream_t)stream);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        set_error("cftg_traj_group_launch: %s", cudaGetErrorString(e));
+        return CFT_ERR_INTERNAL;
+    }
+    return CFT_OK;
+}

@@ -112,6 +112,17 @@ CFT_API cft_status cftg_traj_result(cftg_traj *t, uint32_t *flags_out, uint32_t 
                                     void *stream);
 CFT_API void cftg_traj_free(cftg_traj *t);
 
+/* Several trajectory runs of one device (different programs and formats
+ * allowed) recorded as ONE CUDA graph, each run an independent branch: one
+ * cftg_traj_group_launch puts all of them on the device together. Each
+ * run's flags and STATUS are still read with cftg_traj_result on the
+ * launching stream. The runs must outlive the group. */
+typedef struct cftg_traj_group cftg_traj_group;
+CFT_API cft_status cftg_traj_group_capture(cftg_traj *const *runs, size_t count, void *stream,
+                                           cftg_traj_group **out);
+CFT_API cft_status cftg_traj_group_launch(cftg_traj_group *g, void *stream);
+CFT_API void cftg_traj_group_free(cftg_traj_group *g);
+
 /* Seeded synthetic operands written on the device: n elements of format
  * `fmt` into d_out, 90% normals with unbiased exponents uniform in
  * [-exp_range, exp_range], special_ppm per million specials (+-0,
@@ -151,6 +162,87 @@ CFT_API cft_status cftg_program_run_noalloc(cft_program *prog, const void *d_a, 
                                             uint32_t *flags_out, uint32_t *status_out,
                                             void *stream);
 CFT_API size_t cftg_noalloc_scratch_bytes(void);
+
+/* ---- serving: a continuous-batching request loop ----------------------
+ *
+ * A server owns one device region of hbm_budget bytes and an engine thread.
+ * Requests are element calls (one cftg_call's worth over DEVICE operands the
+ * caller keeps resident) or program requests (`lanes` lanes of a loaded
+ * program run `runs` times each with the scratch block carried, as
+ * cftg_traj_*; initial blocks from the host). The engine admits waiting
+ * requests first come first served per class while a batch slot is free
+ * and the budget holds their outputs (element: n elements; program: the
+ * lanes' state and scratch), and launches each admitted group at once:
+ * element calls as one work-queue launch, requests of one program and bank
+ * as one trajectory launch, each batch on its own stream, up to
+ * max_inflight element and max_program_inflight program batches on the
+ * device together. Requests arriving meanwhile are admitted as slots and
+ * budget free up, so their work overlaps what is running. Results are the
+ * same bits and flags as each call or program run alone.
+ *
+ * A request's output lives in the budget until it completes; with host_out
+ * it is copied there (asynchronously when host_out is pinned memory) before
+ * the completion is posted, and the device copy is then released. Times
+ * are on cftg_clock_ns's clock; t_arrival_ns = 0 takes the submit time. */
+typedef struct cftg_server cftg_server;
+
+typedef struct {
+    size_t struct_size;             /* sizeof(cftg_server_config) */
+    uint64_t hbm_budget;            /* bytes of device memory requests may hold together */
+    uint32_t max_inflight;          /* element batches on the device at once, 1..16 */
+    uint32_t max_program_inflight;  /* program batches on the device at once, 0..16 */
+    uint32_t max_batch_calls;       /* element requests in one batch, 1..2^20 */
+    uint32_t max_batch_lanes;       /* program lanes in one batch, 1..2^24 */
+} cftg_server_config;
+
+#define CFTG_REQ_ELEM    0
+#define CFTG_REQ_PROGRAM 1
+
+typedef struct {
+    size_t struct_size;             /* sizeof(cftg_request) */
+    int type;                       /* CFTG_REQ_ELEM or CFTG_REQ_PROGRAM */
+    int kind, op, fmt, rnd;         /* element requests: as cftg_call */
+    const void *d_a, *d_b, *d_c;    /* element requests: device operands, n elements */
+    size_t n;                       /* element requests: 1..2^30 elements */
+    cft_program *prog;              /* program requests: loaded on the server's device */
+    const void *d_bank;             /* program requests: device bank of a BANK_EXT program */
+    const void *init;               /* program requests: HOST, lanes x n_scratch_out elements */
+    size_t lanes;                   /* program requests: lanes */
+    uint32_t runs;                  /* program requests: runs a lane */
+    void *host_out;                 /* optional HOST destination of the output */
+    uint64_t t_arrival_ns;          /* arrival time (cftg_clock_ns), 0 = now */
+    uint64_t tag;                   /* returned in the completion */
+} cftg_request;
+
+typedef struct {
+    uint64_t tag;
+    int32_t result;                 /* CFT_OK, or why the request failed */
+    uint32_t flags;                 /* the request's IEEE flags */
+    uint32_t status;                /* program requests: STATUS ORed over lanes */
+    uint32_t batch;                 /* the batch that ran it */
+    uint64_t t_arrival_ns, t_admit_ns, t_done_ns;
+} cftg_completion;
+
+typedef struct {
+    uint64_t submitted, completed, failed, batches, launches;
+    uint64_t elements_done, lane_runs_done;
+    uint64_t bytes_in_use, bytes_peak, budget;
+    uint32_t inflight, pending;
+} cftg_server_stats;
+
+CFT_API uint64_t cftg_clock_ns(void);
+CFT_API cft_status cftg_server_create(cft_device *dev, const cftg_server_config *cfg,
+                                      cftg_server **out);
+/* Validates and queues a request (copying it and any initial blocks);
+ * refuses at once a request that needs more than the whole budget. */
+CFT_API cft_status cftg_server_submit(cftg_server *s, const cftg_request *r);
+/* Moves up to cap completions, oldest first, into out; returns how many. */
+CFT_API size_t cftg_server_poll(cftg_server *s, cftg_completion *out, size_t cap);
+/* Waits until every submitted request has completed, up to timeout_ms. */
+CFT_API cft_status cftg_server_drain(cftg_server *s, uint32_t timeout_ms);
+CFT_API void cftg_server_get_stats(cftg_server *s, cftg_server_stats *out);
+/* Finishes every queued request, stops the engine and frees the budget. */
+CFT_API void cftg_server_free(cftg_server *s);
 
 #ifdef __cplusplus
 }

@@ -103,3 +103,40 @@ def test_uneven_trajectories_match_oracle(gpu, oracle, graph):
                 assert np.array_equal(snaps[i, (k + 1) // 2 - 1], s), (i, k)
         assert np.array_equal(final[i * 3:(i + 1) * 3], s), i
     assert fl == acc
+
+
+def test_group_launch_two_programs_two_formats(gpu, oracle):
+    """Lorenz-63 at binary256 and Lorenz-96 at binary128, uneven run counts,
+    as one graph launch (cftg_traj_group_*): every kept state's hash and
+    every final state equal the oracle's segment-by-segment runs."""
+    from cftgb import suites
+    z = np.load(su.GOLD / "odes.npz")
+    progs = []
+    for i, (key, fmt, slots, base, spr, lanes, every) in enumerate(
+            (("l63", 3, 3, 1.0, 100, 45, 2), ("l96", 2, 40, 8.0, 20, 5, 3))):
+        init, runs = suites.ode_lanes(key, fmt, lanes, slots, base, (spr, 8 * spr), spr, 7 + i)
+        progs.append(dict(name=key, image=z[key + "_image"], bank=z[key + "_bank"], fmt=fmt,
+                          slots=slots, init=init, runs=runs, snap_every=every,
+                          max_snaps=int(runs.max()) // every + 1, steps_per_run=spr))
+    res = suites.trajectories(gpu, progs, reps=2)
+    for P, R in zip(progs, res["programs"]):
+        W = wl.words(P["fmt"])
+        slots = P["slots"]
+        img, bank = P["image"].copy(), P["bank"].copy()
+        acc = 0
+        for lane in range(len(P["runs"])):
+            s = P["init"][lane * slots:(lane + 1) * slots].copy()
+            for k in range(int(P["runs"][lane])):
+                out = np.zeros_like(s)
+                A = oracle_lib.SeqArgs()
+                a = np.zeros((1, W), np.uint32)
+                A.a, A.n, A.bank = a.ctypes.data, 1, bank.ctypes.data
+                A.scratch_in, A.scratch_out, A.depth = s.ctypes.data, out.ctypes.data, 256
+                assert oracle.L.sfp_seq_run(img.ctypes.data, img.size, ctypes.byref(A)) == 0
+                acc |= A.flags_out
+                s = out
+                if (k + 1) % P["snap_every"] == 0:
+                    j = (k + 1) // P["snap_every"] - 1
+                    assert hashlib.sha256(TAG + s.tobytes()).digest() == R["_hashes"][lane][j]
+            assert np.array_equal(R["_final"][lane * slots:(lane + 1) * slots], s), (P["name"], lane)
+        assert R["flags"] == acc and R["status"] == 0
