@@ -87,6 +87,13 @@ struct TrajLaunch {
     uint8_t *lane_flags = nullptr;
     uint32_t *lane_status = nullptr;   // n words: each lane's STATUS, or NULL
     uint32_t *word = nullptr;     // [0] flags, [1] status, [2] error
+    // G > 1: each lane served by G threads through a bundle schedule
+    // (bundle.cpp); G == 1: one thread a lane, the plain interpreter
+    int G = 1;
+    uint32_t nb = 0, nloc = 0;                // bundles; a lane's locations
+    const uint64_t *b_ops = nullptr;
+    const uint32_t *b_ctl = nullptr, *b_arg = nullptr;
+    const int32_t *b_match = nullptr;
 };
 
 cudaError_t launch_traj(const TrajLaunch &L, cudaStream_t stream);

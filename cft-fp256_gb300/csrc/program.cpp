@@ -14,6 +14,7 @@
 
 #include "../../include/cft_gb300.h"
 #include "api_core.h"
+#include "bundle.h"
 #include "sha256.h"
 
 using namespace cftg;
@@ -106,6 +107,9 @@ struct cft_program {
     int32_t *d_endrep = nullptr;
     void *d_consts = nullptr;          // the image's constants (not BANK_EXT)
     DevMem bank;                       // a run's bank (BANK_EXT)
+    std::mutex sched_mu;               // schedules for G threads a lane, by G
+    std::map<int, cftg::DevBundles> sched;
+    std::map<int, bool> unschedulable;
 };
 
 namespace {
@@ -591,9 +595,62 @@ extern "C" cft_status cft_program_load(cft_device *dev, const void *image, size_
     return CFT_OK;
 }
 
+cft_status cftg::program_insns(const void *image, size_t bytes, std::vector<uint64_t> &insns,
+                               uint32_t *reach)
+{
+    cft_program tmp;
+    cft_status st = check_image(static_cast<const uint8_t *>(image), bytes, 256u, &tmp);
+    if (st != CFT_OK) return st;
+    insns = tmp.insns;
+    *reach = tmp.P.reach;
+    return CFT_OK;
+}
+
+const DevBundles *cftg::program_bundles(cft_program *pr, int G)
+{
+    std::lock_guard<std::mutex> g(pr->sched_mu);
+    auto it = pr->sched.find(G);
+    if (it != pr->sched.end()) return &it->second;
+    if (pr->unschedulable.count(G)) return nullptr;
+    BundleSchedule s;
+    if (!build_bundles(pr->insns, pr->P.reach, G, s) || !s.nb) {
+        pr->unschedulable[G] = true;
+        return nullptr;
+    }
+    DevBundles d;
+    d.G = G;
+    d.nb = s.nb;
+    d.nloc = s.nloc;
+    d.weighted = s.weighted;
+    d.ops_weighted = s.ops_weighted;
+    void *o = nullptr, *c = nullptr, *a = nullptr, *m = nullptr;
+    cudaSetDevice(pr->dev->ordinal);
+    bool ok = cudaMalloc(&o, s.ops.size() * 8) == cudaSuccess && cudaMalloc(&c, s.nb * 4) == cudaSuccess &&
+              cudaMalloc(&a, s.nb * 4) == cudaSuccess && cudaMalloc(&m, s.nb * 4) == cudaSuccess &&
+              cudaMemcpy(o, s.ops.data(), s.ops.size() * 8, cudaMemcpyHostToDevice) == cudaSuccess &&
+              cudaMemcpy(c, s.ctl.data(), s.nb * 4, cudaMemcpyHostToDevice) == cudaSuccess &&
+              cudaMemcpy(a, s.arg.data(), s.nb * 4, cudaMemcpyHostToDevice) == cudaSuccess &&
+              cudaMemcpy(m, s.match.data(), s.nb * 4, cudaMemcpyHostToDevice) == cudaSuccess;
+    if (!ok) {
+        cudaGetLastError();
+        for (void *p : {o, c, a, m})
+            if (p) cudaFree(p);
+        return nullptr;
+    }
+    d.ops = static_cast<const uint64_t *>(o);
+    d.ctl = static_cast<const uint32_t *>(c);
+    d.arg = static_cast<const uint32_t *>(a);
+    d.match = static_cast<const int32_t *>(m);
+    return &(pr->sched[G] = d);
+}
+
 extern "C" void cft_program_free(cft_program *pr)
 {
     if (!pr) return;
+    for (auto &kv : pr->sched)
+        for (const void *p : {(const void *)kv.second.ops, (const void *)kv.second.ctl,
+                              (const void *)kv.second.arg, (const void *)kv.second.match})
+            cudaFree(const_cast<void *>(p));
     if (pr->d_insns) cudaFree(pr->d_insns);
     if (pr->d_endrep) cudaFree(pr->d_endrep);
     if (pr->d_consts) cudaFree(pr->d_consts);

@@ -500,6 +500,167 @@ __global__ void k_traj(const TrajLaunch L, bool scratch_shared)
     }
 }
 
+// Trajectories with G threads a lane through the bundle schedule
+// (bundle.cpp). A block is one warp holding 32/G lanes; the G threads
+// [li*G, li*G + G) serve lane li. A lane's locations (registers 0..31,
+// scratch slots 32.., renamed values after them) live in shared memory,
+// [(p*W + w)*LPB + li] with one pad word a location so that the group's
+// threads, touching different locations, hit different banks. Each bundle:
+// every thread reads its micro-operation's operands and computes, the warp
+// meets, every thread writes its result, the warp meets again. Only
+// programs without deposits, lane-mask changes, indexed scratch, quiet
+// regions or raises are scheduled, so the lane byte holds the IEEE flags
+// alone and STATUS stays 0.
+template <int FMT>
+__global__ void __launch_bounds__(32) k_traj_g(const TrajLaunch L)
+{
+    constexpr int W = sf::Fmt<FMT>::W;
+    extern __shared__ uint32_t smem[];
+    const SeqProgram &P = L.P;
+    const int G = L.G, LPB = 32 / G;
+    const int t = threadIdx.x, g = t & (G - 1), li = t / G;
+    const size_t local = (size_t)blockIdx.x * LPB + li;
+    const bool have = local < L.n;
+    const size_t lane = have ? (L.order ? L.order[local] : local) : 0;
+    const uint32_t segs = have ? L.segments[lane] : 0u;
+    const int nregs = P.nregs > 0 ? (int)P.nregs : 1;
+    const uint32_t slots = P.n_scratch_out, reach = P.reach;
+    const int RS = W * LPB + 1;
+    auto LOC = [&](uint32_t p, int w) -> uint32_t & { return smem[p * RS + w * LPB + li]; };
+    uint32_t *state = static_cast<uint32_t *>(L.state);
+    uint32_t *snaps = static_cast<uint32_t *>(L.snaps);
+    const uint32_t *kons = static_cast<const uint32_t *>(P.d_consts);
+    if (have) {
+        for (uint32_t sl = g; sl < slots; sl += G) {
+#pragma unroll
+            for (int w = 0; w < W; w++) LOC(32 + sl, w) = state[(lane * slots + sl) * W + w];
+        }
+    }
+    uint32_t flags = 0, err = 0;
+    uint32_t x[W];
+    for (uint32_t seg = 0;; seg++) {
+        const bool mine = have && seg < segs;
+        if (!__any_sync(0xFFFFFFFFu, mine)) break;
+        __syncwarp();
+        for (int r = g; r < nregs; r += G) {
+#pragma unroll
+            for (int w = 0; w < W; w++) LOC(r, w) = 0u;
+        }
+        if (mine) {
+            for (uint32_t sl = slots + g; sl < reach; sl += G) {
+#pragma unroll
+                for (int w = 0; w < W; w++) LOC(32 + sl, w) = 0u;
+            }
+        }
+        __syncwarp();
+        if (mine && g == 0) {
+            if (nregs > 0 && L.a) { load_in<W>(L.a, nullptr, lane, x); for (int w = 0; w < W; w++) LOC(0, w) = x[w]; }
+            if (nregs > 1 && L.b) { load_in<W>(L.b, nullptr, lane, x); for (int w = 0; w < W; w++) LOC(1, w) = x[w]; }
+            if (nregs > 2 && L.c) { load_in<W>(L.c, nullptr, lane, x); for (int w = 0; w < W; w++) LOC(2, w) = x[w]; }
+        }
+        __syncwarp();
+        uint32_t body[4], left[4];
+        int sp = 0;
+        uint32_t b = 0;
+        while (b < L.nb) {
+            const uint32_t kind = __ldg(L.b_ctl + b);
+            if (kind == 0u) {                              // micro-operations
+                const uint64_t u = __ldg(L.b_ops + (size_t)b * G + g);
+                uint32_t res[W];
+                int dest = -1;
+                if (mine && u != ~0ull) {
+                    const uint32_t ia = (uint32_t)(u >> 28) & 0xFFFu;
+                    if ((u >> 14) & 1u) {                  // MOVE
+#pragma unroll
+                        for (int w = 0; w < W; w++) res[w] = LOC(ia, w);
+                    } else {
+                        const uint32_t ib = (uint32_t)(u >> 40) & 0xFFFu, ic = (uint32_t)(u >> 52) & 0xFFFu;
+                        const bool ka = (u >> 11) & 1u, kb = (u >> 12) & 1u, kc = (u >> 13) & 1u;
+                        const int op = (int)(u & 0xFFu), rnd = (int)((u >> 8) & 7u);
+                        uint32_t va[W], vb[W], vc[W], fl = 0u;
+#pragma unroll
+                        for (int w = 0; w < W; w++) {
+                            va[w] = ka ? __ldg(kons + ia * W + w) : LOC(ia, w);
+                            vb[w] = kb ? __ldg(kons + ib * W + w) : LOC(ib, w);
+                            vc[w] = kc ? __ldg(kons + ic * W + w) : LOC(ic, w);
+                        }
+                        if (op <= 3) sf::arith_rt<FMT>(op, va, vb, vc, rnd, res, fl);
+                        else sf::simple<FMT>(op, va, vb, vc, res, fl);
+                        flags |= fl;
+                    }
+                    dest = (int)((u >> 16) & 0xFFFu);
+                }
+                __syncwarp();
+                if (dest >= 0) {
+#pragma unroll
+                    for (int w = 0; w < W; w++) LOC((uint32_t)dest, w) = res[w];
+                }
+                __syncwarp();
+                b++;
+            } else if (kind == 1u) {                       // REPEAT
+                const bool any = __any_sync(0xFFFFFFFFu, mine);
+                const uint32_t imm = __ldg(L.b_arg + b);
+                if (imm == 0u || !any) {
+                    b = (uint32_t)__ldg(L.b_match + b) + 1u;
+                } else if (sp >= 4) {
+                    err |= 1u;
+                    break;
+                } else {
+                    body[sp] = b + 1;
+                    left[sp] = imm;
+                    sp++;
+                    b++;
+                }
+            } else if (kind == 2u) {                       // ENDREP
+                const bool any = __any_sync(0xFFFFFFFFu, mine);
+                if (sp <= 0) {
+                    err |= 2u;
+                    break;
+                }
+                left[sp - 1]--;
+                if (left[sp - 1] > 0u && any) {
+                    b = body[sp - 1];
+                } else {
+                    sp--;
+                    b++;
+                }
+            } else {                                       // HALT
+                break;
+            }
+        }
+        __syncwarp();
+        if (mine && snaps && L.snap_every && (seg + 1) % L.snap_every == 0) {
+            const uint32_t k = (seg + 1) / L.snap_every - 1;
+            if (k < L.max_snaps) {
+                for (uint32_t sl = g; sl < slots; sl += G) {
+#pragma unroll
+                    for (int w = 0; w < W; w++)
+                        snaps[((lane * L.max_snaps + k) * slots + sl) * W + w] = LOC(32 + sl, w);
+                }
+            }
+        }
+    }
+    __syncwarp();
+    if (have) {
+        for (uint32_t sl = g; sl < slots; sl += G) {
+#pragma unroll
+            for (int w = 0; w < W; w++) state[(lane * slots + sl) * W + w] = LOC(32 + sl, w);
+        }
+    }
+    uint32_t lf = flags;                                   // the lane's G threads
+    for (int o = 1; o < G; o <<= 1) lf |= __shfl_xor_sync(0xFFFFFFFFu, lf, o);
+    if (have && g == 0) {
+        if (L.lane_flags) L.lane_flags[lane] = (uint8_t)(lf & 0x1Fu);
+        if (L.lane_status) L.lane_status[lane] = 0u;
+    }
+    flags = __reduce_or_sync(0xFFFFFFFFu, flags);
+    err = __reduce_or_sync(0xFFFFFFFFu, err);
+    if (t == 0) {
+        if (flags) atomicOr(L.word + 0, flags);
+        if (err) atomicOr(L.word + 2, err);
+    }
+}
+
 template <int FMT>
 static int seq_threads(const SeqProgram &P, size_t *smem)
 {
@@ -541,9 +702,31 @@ static cudaError_t go_traj(const TrajLaunch &L, cudaStream_t s)
     return cudaGetLastError();
 }
 
+template <int FMT>
+static cudaError_t go_traj_g(const TrajLaunch &L, cudaStream_t s)
+{
+    constexpr int W = sf::Fmt<FMT>::W;
+    const int LPB = 32 / L.G;
+    const size_t smem = (size_t)L.nloc * (size_t)(W * LPB + 1) * 4;
+    cudaError_t e = cudaFuncSetAttribute(k_traj_g<FMT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    const size_t blocks = (L.n + LPB - 1) / LPB;
+    k_traj_g<FMT><<<(unsigned)blocks, 32, smem, s>>>(L);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_traj(const TrajLaunch &L, cudaStream_t s)
 {
     if (L.n == 0) return cudaSuccess;
+    if (L.G > 1 && L.nb) {
+        switch (L.P.fmt) {
+        case 0: return go_traj_g<0>(L, s);
+        case 1: return go_traj_g<1>(L, s);
+        case 2: return go_traj_g<2>(L, s);
+        default: return go_traj_g<3>(L, s);
+        }
+    }
     switch (L.P.fmt) {
     case 0: return go_traj<0>(L, s);
     case 1: return go_traj<1>(L, s);

@@ -28,6 +28,7 @@
 #include "../../include/cft_gb300.h"
 #include "api_core.h"
 #include "arena.h"
+#include "bundle.h"
 #include "queue.h"
 
 using namespace cftg;
@@ -270,6 +271,7 @@ bool cftg_server::launch_prog(Slot &sl)
     T.lane_flags = sl.d_lflags;
     T.lane_status = sl.d_lstatus;
     T.word = sl.d_word;
+    plan_lanes(head->r.prog, lanes, T);
     if (e == cudaSuccess) e = launch_traj(T, sl.s);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(sl.h_lflags, sl.d_lflags, lanes, cudaMemcpyDeviceToHost, sl.s);

@@ -13,6 +13,7 @@
 
 #include "../../include/cft_gb300.h"
 #include "api_core.h"
+#include "bundle.h"
 
 using namespace cftg;
 
@@ -116,6 +117,7 @@ extern "C" cft_status cftg_traj_create(cft_program *prog, const uint32_t *segmen
     L.scratch = t->d_scratch;
     L.lane_flags = d_lane_flags;
     L.word = t->d_word;
+    plan_lanes(prog, n, L);
     *out = t;
     return CFT_OK;
 }

@@ -112,6 +112,22 @@ CFT_API cft_status cftg_traj_result(cftg_traj *t, uint32_t *flags_out, uint32_t 
                                     void *stream);
 CFT_API void cftg_traj_free(cftg_traj *t);
 
+/* A trajectory launch of few lanes spreads each lane over G threads
+ * (G = 1, 2, 4, ... 32, chosen per launch from the lane count and the
+ * program's parallelism): every straight-line stretch of the program is
+ * scheduled into bundles of at most G independent operations, run
+ * together, each reading its operands before any writes its result. Only
+ * programs whose control is REPEAT/ENDREP/HALT and whose scratch accesses
+ * are LDL/STL are scheduled; results are those of one thread a lane.
+ * cftg_program_schedule returns that schedule for an image, with no device:
+ * ops (nb x G instruction words, all ones where a thread idles), ctl (0
+ * operations, 1 REPEAT, 2 ENDREP, 3 HALT), arg (REPEAT counts) and match
+ * (REPEAT <-> ENDREP bundle). The arrays are filled when cap >= *nb;
+ * CFT_ERR_UNSUPPORTED for a program outside the scheduled set. */
+CFT_API cft_status cftg_program_schedule(const void *image, size_t bytes, uint32_t G,
+                                         uint64_t *ops, uint32_t *ctl, uint32_t *arg,
+                                         int32_t *match, size_t cap, size_t *nb);
+
 /* Several trajectory runs of one device (different programs and formats
  * allowed) recorded as ONE CUDA graph, each run an independent branch: one
  * cftg_traj_group_launch puts all of them on the device together. Each

@@ -1,0 +1,129 @@
+"""The bundle schedule (G threads a lane, cftg_program_schedule) replayed on
+the host: each bundle's operations read their operands, then all write,
+with the oracle's arithmetic (sfp_compute). The state and flags after a run
+must equal the oracle's own sequencer (sfp_seq_run) on the same lanes, for
+every G - a check of the scheduler's dependence rules with no GPU."""
+import ctypes
+
+import numpy as np
+import pytest
+
+import cftgb
+import oracle_lib
+import seq_util as su
+from cftgb import suites, workload as wl
+
+NOP = (1 << 64) - 1
+
+
+def schedule(img, G):
+    L = cftgb.lib()
+    vp = ctypes.c_void_p
+    L.cftg_program_schedule.argtypes = [vp, ctypes.c_size_t, ctypes.c_uint32, vp, vp, vp, vp,
+                                        ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]
+    nb = ctypes.c_size_t()
+    st = L.cftg_program_schedule(img.ctypes.data, img.size, G, None, None, None, None, 0,
+                                 ctypes.byref(nb))
+    if st:
+        return None
+    n = nb.value
+    ops = np.zeros(n * G, np.uint64)
+    ctl = np.zeros(n, np.uint32)
+    arg = np.zeros(n, np.uint32)
+    match = np.zeros(n, np.int32)
+    assert L.cftg_program_schedule(img.ctypes.data, img.size, G, ops.ctypes.data, ctl.ctypes.data,
+                                   arg.ctypes.data, match.ctypes.data, n, ctypes.byref(nb)) == 0
+    return ops.reshape(n, G), ctl, arg, match
+
+
+def replay(oracle, sched, fmt, bank, block, reach, W):
+    """One run of one lane through the schedule; returns (scratch, flags).
+    Locations: registers 0..31, scratch slots 32.., renamed values after."""
+    ops, ctl, arg, match = sched
+    loc = np.zeros((4096, W), np.uint32)
+    loc[32:32 + len(block)] = block
+    kons = bank.view(np.uint32).reshape(-1, W) if bank is not None and bank.size else None
+    flags = 0
+    b, stack = 0, []
+    out = np.zeros(W, np.uint32)
+    fl = ctypes.c_uint32()
+    while b < len(ctl):
+        if ctl[b] == 0:
+            writes = []
+            for u in ops[b]:
+                u = int(u)
+                if u == NOP:
+                    continue
+                dest, ia, ib, ic = (u >> 16) & 0xFFF, (u >> 28) & 0xFFF, (u >> 40) & 0xFFF, (u >> 52) & 0xFFF
+                if (u >> 14) & 1:                     # MOVE
+                    writes.append((dest, loc[ia].copy()))
+                    continue
+                vals = [np.ascontiguousarray(kons[i] if (u >> (11 + k)) & 1 else loc[i])
+                        for k, i in enumerate((ia, ib, ic))]
+                assert oracle.L.sfp_compute(fmt, u & 0xFF, (u >> 8) & 7, vals[0].ctypes.data,
+                                            vals[1].ctypes.data, vals[2].ctypes.data,
+                                            out.ctypes.data, ctypes.byref(fl)) == 0
+                flags |= fl.value
+                writes.append((dest, out.copy()))
+            for where, v in writes:
+                loc[where] = v
+            b += 1
+        elif ctl[b] == 1:
+            if arg[b] == 0:
+                b = int(match[b]) + 1
+            else:
+                stack.append([b + 1, int(arg[b])])
+                b += 1
+        elif ctl[b] == 2:
+            stack[-1][1] -= 1
+            if stack[-1][1] > 0:
+                b = stack[-1][0]
+            else:
+                stack.pop()
+                b += 1
+        else:
+            break
+    return loc[32:32 + reach], flags
+
+
+ODES = [("l63", 3, 3, 1.0), ("l96", 2, 40, 8.0), ("hh", 3, 4, None)]
+
+
+@pytest.mark.parametrize("key,fmt,slots,base", ODES, ids=[o[0] for o in ODES])
+@pytest.mark.parametrize("G", [1, 2, 4, 8, 32])
+def test_schedule_replay_equals_sequencer(oracle, key, fmt, slots, base, G):
+    oracle.L.sfp_compute.argtypes = [ctypes.c_int] * 3 + [ctypes.c_void_p] * 4 + [
+        ctypes.POINTER(ctypes.c_uint32)]
+    z = np.load(su.GOLD / "odes.npz")
+    img, bank = z[key + "_image"].copy(), z[key + "_bank"].copy()
+    sched = schedule(img, G)
+    assert sched is not None
+    ops = sched[0]
+    assert (ops != np.uint64(NOP)).sum(axis=1).max() <= G
+    W = wl.words(fmt)
+    if base is None:
+        init = suites.hh_init(1, 9)
+    else:
+        init, _ = suites.ode_lanes(key, fmt, 1, slots, base, (100, 100), 100, 3)
+    got, gflags = replay(oracle, sched, fmt, bank, init, 256, W)
+    out = np.zeros_like(init)
+    A = oracle_lib.SeqArgs()
+    a = np.zeros((1, W), np.uint32)
+    A.a, A.n, A.bank = a.ctypes.data, 1, bank.ctypes.data
+    A.scratch_in, A.scratch_out, A.depth = init.ctypes.data, out.ctypes.data, 256
+    assert oracle.L.sfp_seq_run(img.ctypes.data, img.size, ctypes.byref(A)) == 0
+    assert np.array_equal(got[:slots], out), f"{key} G={G}"
+    assert gflags == A.flags_out
+
+
+def test_schedule_parallelism():
+    """The schedule actually finds parallel work: Lorenz-96 (40 independent
+    components) fills wide bundles; and a program outside the scheduled set
+    (one that deposits) is refused."""
+    z = np.load(su.GOLD / "odes.npz")
+    img = z["l96_image"].copy()
+    n1 = len(schedule(img, 1)[1])
+    n32 = len(schedule(img, 32)[1])
+    assert n32 * 8 < n1, (n1, n32)
+    dep = next(p for p in su.cases() if su.header(su.load(p)["image"])["maxdep"] > 0)
+    assert schedule(su.load(dep)["image"].copy(), 4) is None

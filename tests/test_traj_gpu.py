@@ -73,8 +73,17 @@ def test_certificate_segments_as_one_trajectory_launch(gpu):
     assert fl == int(np.bitwise_or.reduce(z["flags"])) and st == 0
 
 
+@pytest.fixture(params=["auto", "1", "2", "4", "32"])
+def lane_threads(request, monkeypatch):
+    """Threads a lane for the trajectory launches: the planner's choice, or
+    forced (1 = the plain interpreter, else the bundle schedule)."""
+    if request.param != "auto":
+        monkeypatch.setenv("CFTG_LANE_THREADS", request.param)
+    return request.param
+
+
 @pytest.mark.parametrize("graph", [False, True])
-def test_uneven_trajectories_match_oracle(gpu, oracle, graph):
+def test_uneven_trajectories_match_oracle(gpu, oracle, graph, lane_threads):
     z = np.load(su.GOLD / "lorenz63_cert.npz")
     img, bank = z["image"].copy(), z["bank"].copy()
     rng = np.random.default_rng(5)
@@ -105,7 +114,7 @@ def test_uneven_trajectories_match_oracle(gpu, oracle, graph):
     assert fl == acc
 
 
-def test_group_launch_two_programs_two_formats(gpu, oracle):
+def test_group_launch_two_programs_two_formats(gpu, oracle, lane_threads):
     """Lorenz-63 at binary256 and Lorenz-96 at binary128, uneven run counts,
     as one graph launch (cftg_traj_group_*): every kept state's hash and
     every final state equal the oracle's segment-by-segment runs."""
