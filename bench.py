@@ -43,6 +43,9 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT / "cft-fp256_gb300"))
 
 METRIC = "fp256/fp128 FMA Gelem/s bit-exact (plain vs batched); mixed-load p50/p99 latency"
+# DRAM bytes (read + write) an element of the FMA kernel, from the ncu
+# capture summarised in profiles/k_elem_fma256_n4M.md (518.3 MB / 4,194,304)
+TRAFFIC_B_PER_ELEM = {3: 518.3e6 / 4194304}
 N_DEFAULT = 1 << 24
 
 
@@ -337,6 +340,12 @@ def main():
                     help="trajectories suite: also time each program's launch alone")
     ap.add_argument("--rate", type=float, default=20000.0,
                     help="offered requests a second of the serving suite")
+    ap.add_argument("--program-frac", type=float, default=0.02,
+                    help="serving suite: fraction of requests that are program ensembles")
+    ap.add_argument("--inflight", type=int, default=6,
+                    help="serving suite: element batches on the device at once")
+    ap.add_argument("--program-inflight", type=int, default=6,
+                    help="serving suite: program batches on the device at once")
     ap.add_argument("--seconds", type=float, default=60.0,
                     help="length of the serving suite's request stream")
     ap.add_argument("--fmt", type=int, default=3, help="format of the headline leg (3 = binary256)")
@@ -360,7 +369,9 @@ def main():
         elif args.suite == "serving":
             z = np.load(ROOT / "tests" / "golden" / "odes.npz")
             print(json.dumps(suites.serving(h, z["hh_image"], z["hh_bank"], rate=args.rate,
-                                            seconds=args.seconds)))
+                                            seconds=args.seconds, program_frac=args.program_frac,
+                                            max_inflight=args.inflight,
+                                            max_program_inflight=args.program_inflight)))
         else:
             print(json.dumps(getattr(suites, args.suite)(h)))
         cftgb.close_device(h)
@@ -368,6 +379,7 @@ def main():
 
     import torch
     import cftgb
+    from cftgb import algorithmic as alg
     from cftgb import workload as wl
 
     ws, rank, local = dist_init()
@@ -502,9 +514,20 @@ def main():
                     "d2h_bytes_per_step": 32 * n + 8, "path": "cft_run, pinned host buffers",
                     "steps": e2e_steps},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                         "frac": achieved / hbm_peak, "traffic": None,
+                         "frac": achieved / hbm_peak,
+                         "traffic": (TRAFFIC_B_PER_ELEM[fmt] * n) if fmt in TRAFFIC_B_PER_ELEM else None,
+                         "traffic_source": "dram read+write bytes per element of one ncu capture "
+                                           "(n = 4,194,304) scaled to n",
                          "peak_source": peak_kind,
-                         "note": "integer-pipe bound kernel: algorithmic 128 B/element"},
+                         "note": f"integer-pipe bound kernel: algorithmic {4 * 4 * wl.words(fmt)} "
+                                 "B/element"},
+            "int_pipe": {"alg_ops_per_elem": alg.int_ops(fmt, "fma"),
+                         "achieved_tops": value / ws * alg.int_ops(fmt, "fma") / 1e3,
+                         "issue_peak_tops": alg.int_issue_peak_tops(),
+                         "frac": value / ws * alg.int_ops(fmt, "fma") / 1e3 / alg.int_issue_peak_tops(),
+                         "note": "algorithmic integer operations (2L^2 product halves + 8L) over "
+                                 "the nominal issue rate 152 SMs x 128 lanes x 2070 MHz; no "
+                                 "measured integer peak exists"},
             "cpu_baseline": cpu,
             "gpu_launches": args.steps,
             "clocks": clk.summary(),

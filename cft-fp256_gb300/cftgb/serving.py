@@ -12,7 +12,8 @@ vp = ctypes.c_void_p
 class ServerConfig(ctypes.Structure):
     _fields_ = [("struct_size", ctypes.c_size_t), ("hbm_budget", ctypes.c_uint64),
                 ("max_inflight", ctypes.c_uint32), ("max_program_inflight", ctypes.c_uint32),
-                ("max_batch_calls", ctypes.c_uint32), ("max_batch_lanes", ctypes.c_uint32)]
+                ("max_batch_calls", ctypes.c_uint32), ("max_batch_lanes", ctypes.c_uint32),
+                ("max_batch_elements", ctypes.c_uint64)]
 
 
 class Request(ctypes.Structure):
@@ -35,7 +36,9 @@ class Stats(ctypes.Structure):
     _fields_ = [(k, ctypes.c_uint64) for k in ("submitted", "completed", "failed", "batches",
                                                "launches", "elements_done", "lane_runs_done",
                                                "bytes_in_use", "bytes_peak", "budget")] + \
-               [("inflight", ctypes.c_uint32), ("pending", ctypes.c_uint32)]
+               [("inflight", ctypes.c_uint32), ("pending", ctypes.c_uint32),
+                ("engine_launch_ns", ctypes.c_uint64), ("engine_retire_ns", ctypes.c_uint64),
+                ("slot_full_turns", ctypes.c_uint64)]
 
 
 REQ_ELEM, REQ_PROGRAM = 0, 1
@@ -72,11 +75,11 @@ class Server:
     it after every queued request has finished."""
 
     def __init__(self, h, budget, max_inflight=4, max_program_inflight=4, max_batch_calls=4096,
-                 max_batch_lanes=65536):
+                 max_batch_lanes=65536, max_batch_elements=0):
         self.L = _lib.lib()
         _bind(self.L)
         cfg = ServerConfig(ctypes.sizeof(ServerConfig), budget, max_inflight, max_program_inflight,
-                           max_batch_calls, max_batch_lanes)
+                           max_batch_calls, max_batch_lanes, max_batch_elements)
         self.s = vp()
         _lib.check(self.L.cftg_server_create(h, ctypes.byref(cfg), ctypes.byref(self.s)),
                    "cftg_server_create")

@@ -369,7 +369,7 @@ def hh_init(lanes, seed):
 
 def serving(h, hh_image, hh_bank, rate=20000.0, seconds=60.0, seed=5, budget=40 << 30,
             program_frac=0.02, hh_lanes=32, max_log2=22, sample_every=2000, max_inflight=6,
-            max_program_inflight=6):
+            max_program_inflight=6, max_batch_elements=1 << 24):
     """Open-loop serving: requests arrive as a Poisson stream of `rate` a
     second for `seconds`; each is an element call (binary128 or binary256
     1:1, size log-uniform in [64, 2^max_log2], operation uniform over add,
@@ -425,7 +425,8 @@ def serving(h, hh_image, hh_bank, rate=20000.0, seconds=60.0, seed=5, budget=40 
     req = sv.Request()
     comp = []
     with sv.Server(h, budget, max_inflight=max_inflight, max_program_inflight=max_program_inflight,
-                   max_batch_calls=4096, max_batch_lanes=1 << 16) as srv:
+                   max_batch_calls=4096, max_batch_lanes=1 << 16,
+                   max_batch_elements=max_batch_elements) as srv:
         t0 = sv.clock_ns() + 20_000_000
         arr_ns = (t0 + arrive * 1e9).astype(np.int64)
         i = loops = 0
@@ -480,6 +481,7 @@ def serving(h, hh_image, hh_bank, rate=20000.0, seconds=60.0, seed=5, budget=40 
         stats = srv.stats()
     done = np.concatenate(comp)
     lat = (done["t_done_ns"].astype(np.int64) - done["t_arrival_ns"].astype(np.int64)) / 1e6
+    wait = (done["t_admit_ns"].astype(np.int64) - done["t_arrival_ns"].astype(np.int64)) / 1e6
     tags = done["tag"].astype(np.int64)
     prog_mask = is_prog[tags]
 
@@ -525,6 +527,14 @@ def serving(h, hh_image, hh_bank, rate=20000.0, seconds=60.0, seed=5, budget=40 
         "program_lane_steps_per_s": lane_steps / wall,
         "latency_all": pct(lat), "latency_elem": pct(lat[~prog_mask]),
         "latency_program": pct(lat[prog_mask]),
+        "admission_wait_elem": pct(wait[~prog_mask]),
+        "admission_wait_program": pct(wait[prog_mask]),
+        "batch_requests_mean": float(len(done) / max(1, stats["batches"])),
+        "engine": {"launch_s": stats["engine_launch_ns"] / 1e9,
+                   "retire_s": stats["engine_retire_ns"] / 1e9,
+                   "slot_full_turns": int(stats["slot_full_turns"]),
+                   "max_inflight": max_inflight, "max_program_inflight": max_program_inflight,
+                   "max_batch_elements": max_batch_elements},
         "batches": int(stats["batches"]), "bytes_peak": int(stats["bytes_peak"]),
         "budget": int(budget), "samples_checked": len(samples), "sample_mismatches": bad,
         "bit_exact_alone_vs_mix": not bad,

@@ -131,9 +131,12 @@ bool cftg_server::launch_elem(Slot &sl)
 {
     sl.reqs.clear();
     const uint64_t t = now_ns();
+    uint64_t elems = 0;
     while (!elem_q.empty() && sl.reqs.size() < cfg.max_batch_calls) {
         Req *q = elem_q.front();
+        if (cfg.max_batch_elements && !sl.reqs.empty() && elems + q->r.n > cfg.max_batch_elements) break;
         if (!arena.alloc(q->out_bytes, &q->off)) break;
+        elems += q->r.n;
         elem_q.pop_front();
         q->t_admit = t;
         sl.reqs.push_back(q);
@@ -367,6 +370,7 @@ void cftg_server::loop()
             st.pending = (uint32_t)(elem_q.size() + prog_q.size());
         }
         bool did = false;
+        const uint64_t t0 = now_ns();
         for (auto &sl : slots) {
             if (!sl.busy) continue;
             const cudaError_t e = cudaEventQuery(sl.ev);
@@ -374,18 +378,27 @@ void cftg_server::loop()
             retire(sl, e);
             did = true;
         }
-        bool can_wait_memory = false;
+        const uint64_t t1 = now_ns();
+        bool full = !elem_q.empty() || !prog_q.empty();
         for (size_t i = 0; i < ne && !elem_q.empty(); i++)
             if (!slots[i].busy) {
+                full = false;
                 if (launch_elem(slots[i])) did = true;
-                else { can_wait_memory = true; break; }
+                else break;                          // the budget is short: wait for a retire
             }
         for (size_t i = ne; i < slots.size() && !prog_q.empty(); i++)
             if (!slots[i].busy) {
+                full = false;
                 if (launch_prog(slots[i])) did = true;
-                else { can_wait_memory = true; break; }
+                else break;
             }
-        (void)can_wait_memory;
+        const uint64_t t2 = now_ns();
+        {
+            std::lock_guard<std::mutex> g(mu);
+            st.engine_retire_ns += t1 - t0;
+            st.engine_launch_ns += t2 - t1;
+            if (full) st.slot_full_turns++;
+        }
         {
             std::lock_guard<std::mutex> g(mu);
             uint32_t inflight = 0;

@@ -228,14 +228,16 @@ extern "C" cft_status cftg_traj_group_capture(cftg_traj *const *runs, size_t cou
     }
     if (e == cudaSuccess) e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
+        // fork: every run after the first on its own captured stream, the
+        // first on `stream`; then join them all back into `stream`
         cudaError_t e2 = cudaEventRecord(fork, s);
         for (size_t i = 1; e2 == cudaSuccess && i < count; i++) {
             e2 = cudaStreamWaitEvent(side[i], fork, 0);
             if (e2 == cudaSuccess) e2 = traj_enqueue(runs[i], side[i]);
             if (e2 == cudaSuccess) e2 = cudaEventRecord(join[i], side[i]);
-            if (e2 == cudaSuccess) e2 = cudaStreamWaitEvent(s, join[i], 0);
         }
         if (e2 == cudaSuccess) e2 = traj_enqueue(runs[0], s);
+        for (size_t i = 1; e2 == cudaSuccess && i < count; i++) e2 = cudaStreamWaitEvent(s, join[i], 0);
         e = cudaStreamEndCapture(s, &g->graph);
         if (e2 != cudaSuccess) e = e2;
     }

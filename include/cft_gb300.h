@@ -119,11 +119,17 @@ CFT_API void cftg_traj_free(cftg_traj *t);
  * together, each reading its operands before any writes its result. Only
  * programs whose control is REPEAT/ENDREP/HALT and whose scratch accesses
  * are LDL/STL are scheduled; results are those of one thread a lane.
+ * Within a stretch each written value gets a location of its own, so only
+ * true dependences order operations; LDL/STL become renames.
  * cftg_program_schedule returns that schedule for an image, with no device:
- * ops (nb x G instruction words, all ones where a thread idles), ctl (0
+ * ops (nb x G micro-operations, all ones where a thread idles), ctl (0
  * operations, 1 REPEAT, 2 ENDREP, 3 HALT), arg (REPEAT counts) and match
- * (REPEAT <-> ENDREP bundle). The arrays are filled when cap >= *nb;
- * CFT_ERR_UNSUPPORTED for a program outside the scheduled set. */
+ * (REPEAT <-> ENDREP bundle). A micro-operation names locations (registers
+ * 0..31, scratch slots 32.., renamed values after them): bits 0-7 opcode,
+ * 8-10 rounding attribute, 11-13 operand a/b/c is a constant index, 14 MOVE
+ * (dest = a), 16-27 dest, 28-39 a, 40-51 b, 52-63 c. The arrays are filled
+ * when cap >= *nb; CFT_ERR_UNSUPPORTED for a program outside the scheduled
+ * set. */
 CFT_API cft_status cftg_program_schedule(const void *image, size_t bytes, uint32_t G,
                                          uint64_t *ops, uint32_t *ctl, uint32_t *arg,
                                          int32_t *match, size_t cap, size_t *nb);
@@ -209,6 +215,9 @@ typedef struct {
     uint32_t max_program_inflight;  /* program batches on the device at once, 0..16 */
     uint32_t max_batch_calls;       /* element requests in one batch, 1..2^20 */
     uint32_t max_batch_lanes;       /* program lanes in one batch, 1..2^24 */
+    uint64_t max_batch_elements;    /* elements of one element batch (0: no limit); a batch
+                                       completes as a whole, so this bounds the wait of its
+                                       smallest requests */
 } cftg_server_config;
 
 #define CFTG_REQ_ELEM    0
@@ -244,6 +253,8 @@ typedef struct {
     uint64_t elements_done, lane_runs_done;
     uint64_t bytes_in_use, bytes_peak, budget;
     uint32_t inflight, pending;
+    uint64_t engine_launch_ns, engine_retire_ns;   /* engine thread time spent */
+    uint64_t slot_full_turns;       /* engine turns that found work waiting and no free slot */
 } cftg_server_stats;
 
 CFT_API uint64_t cftg_clock_ns(void);
