@@ -318,11 +318,11 @@ extern "C" void cft_close(cft_device *dev)
 }
 
 // Sequencer features this executor implements (reference cft.h:785-1030):
-// everything the software backend publishes except augmented addition and
-// the segmented reductions, which this backend does not carry.
+// everything the software backend publishes except augmented addition,
+// which this backend does not carry; the segmented reductions included.
 static const uint32_t SEQ_FEATURES =
     CFT_SEQ_FEAT_WIDE_CONST | CFT_SEQ_FEAT_REGS32 | CFT_SEQ_FEAT_BANK_PTR | CFT_SEQ_FEAT_KX9 |
-    CFT_ALU_EXT_IMUL | CFT_SEQ_FEAT_SCRATCH | CFT_SEQ_FEAT_SCRATCH_IO |
+    CFT_ALU_EXT_IMUL | CFT_SEQ_FEAT_SCRATCH | CFT_SEQ_FEAT_SCRATCH_IO | CFT_FEAT_REDUCE_SEG |
     CFT_SEQ_FEAT_SCRATCH_STRICT | CFT_SEQ_FEAT_SCALAR | CFT_SEQ_FEAT_INDEXED |
     CFT_SEQ_FEAT_LANE_MASK | CFT_SEQ_FEAT_SCRATCH_STEP | CFT_SEQ_FEAT_LANE_FLAGS |
     CFT_SEQ_FEAT_FLAG_CONTROL;
@@ -367,7 +367,6 @@ extern "C" int cft_supports(cft_device *dev, cft_op op, cft_format fmt)
     if (!dev || (int)fmt < 0 || (int)fmt > 3) return 0;
     const int o = (int)op;
     if (!op_assigned(o)) return 0;
-    if (op_is_reduction(o)) return 0;      // cft_reduce is not carried here
     return 1;
 }
 

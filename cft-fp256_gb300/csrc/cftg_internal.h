@@ -39,6 +39,34 @@ cudaError_t launch_elem(const ElemLaunch &L, cudaStream_t stream);
 // The kernels' dimensions for a given launch (used by the queue autotuner).
 int sm_count();
 
+// ---- reductions (reduce.cu) -------------------------------------------------
+
+enum RedMode : int { RED_SUM = 0, RED_DOT = 1, RED_SQ = 2, RED_ABS = 3, RED_MAX = 4 };
+
+// One level of the tree's leftover items: [start, start + len) of `src`
+// (leaves from the call's a/b when `leaf`).
+struct RedLevel {
+    const void *src;
+    size_t start;
+    uint32_t len;
+    bool leaf;
+};
+struct RedLevels {
+    const void *a, *b;
+    int count;
+    RedLevel lev[8];
+};
+
+// Elements of partial results a tree over n items needs.
+size_t red_partial_elems(size_t n);
+// d_out (one element) = the reduction of a/b[0, n) (n >= 1); word[0] gets
+// the flags. partials: red_partial_elems(n) elements of device memory.
+cudaError_t launch_reduce(int fmt, int mode, const void *a, const void *b, size_t n,
+                          void *partials, void *out, int rnd, uint32_t *word, cudaStream_t s);
+// out[s] = the reduction of slice s of `seg` elements, s < nseg; *word |= flags.
+cudaError_t launch_reduce_seg(int fmt, int mode, const void *a, const void *b, size_t nseg,
+                              size_t seg, void *out, int rnd, uint32_t *word, cudaStream_t s);
+
 // ---- the sequencer ------------------------------------------------------
 
 // A loaded program as the GPU executor reads it (built by program.cpp).

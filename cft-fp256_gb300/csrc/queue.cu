@@ -164,10 +164,25 @@ __global__ void __launch_bounds__(256) k_queue_calls(const QCall *__restrict__ c
     }
 }
 
+// Long trajectory launches share the SMs with the work queue in the serving
+// loop; both kernels ask for the same L1/shared split, so that an SM holding
+// one can take blocks of the other without draining to change it.
+static void carveout_once()
+{
+    static bool done = false;
+    if (done) return;
+    done = true;
+    cudaFuncSetAttribute(k_queue_calls, cudaFuncAttributePreferredSharedMemoryCarveout,
+                         cudaSharedmemCarveoutMaxShared);
+    cudaFuncSetAttribute(k_queue, cudaFuncAttributePreferredSharedMemoryCarveout,
+                         cudaSharedmemCarveoutMaxShared);
+}
+
 cudaError_t launch_queue_calls(const QCall *calls, const uint32_t *prefix, uint32_t ncalls,
                                uint32_t *counter, uint32_t *call_flags, int blocks, cudaStream_t s)
 {
     if (ncalls == 0) return cudaSuccess;
+    carveout_once();
     k_queue_calls<<<blocks, 256, 0, s>>>(calls, prefix, ncalls, counter, call_flags);
     return cudaGetLastError();
 }

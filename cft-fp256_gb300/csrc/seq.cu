@@ -696,6 +696,9 @@ static cudaError_t go_traj(const TrajLaunch &L, cudaStream_t s)
     if (shared) smem += scr * T;
     cudaError_t e = cudaFuncSetAttribute(k_traj<FMT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_traj<FMT>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 cudaSharedmemCarveoutMaxShared);
     if (e != cudaSuccess) return e;
     const size_t blocks = (L.n + T - 1) / T;
     k_traj<FMT><<<(unsigned)blocks, T, smem, s>>>(L, shared);
@@ -710,6 +713,9 @@ static cudaError_t go_traj_g(const TrajLaunch &L, cudaStream_t s)
     const size_t smem = (size_t)L.nloc * (size_t)(W * LPB + 1) * 4;
     cudaError_t e = cudaFuncSetAttribute(k_traj_g<FMT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_traj_g<FMT>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 cudaSharedmemCarveoutMaxShared);
     if (e != cudaSuccess) return e;
     const size_t blocks = (L.n + LPB - 1) / LPB;
     k_traj_g<FMT><<<(unsigned)blocks, 32, smem, s>>>(L);

@@ -35,6 +35,8 @@ using namespace cftg;
 
 namespace {
 
+constexpr size_t SERVE_INIT_STAGING = 16u << 20;   // a program slot's pinned initial blocks
+
 uint64_t now_ns()
 {
     return (uint64_t)std::chrono::duration_cast<std::chrono::nanoseconds>(
@@ -66,6 +68,8 @@ struct Slot {
     uint32_t *h_seg = nullptr, *d_seg = nullptr, *h_order = nullptr, *d_order = nullptr;
     uint32_t *h_lstatus = nullptr, *d_lstatus = nullptr, *d_word = nullptr, *h_word = nullptr;
     uint8_t *h_lflags = nullptr, *d_lflags = nullptr;
+    uint8_t *h_init = nullptr;       // pinned staging of the initial blocks
+    size_t h_init_cap = 0;
     size_t prog_off = 0, prog_bytes = 0;
     std::vector<Req *> reqs;
     std::vector<size_t> lane0;
@@ -79,6 +83,12 @@ struct cftg_server {
     void *base = nullptr;           // the budget's device region
     Arena arena;
     std::vector<Slot> slots;        // [0, max_inflight) element, the rest program
+    // Few streams, shared by the slots: a GPU runs work from a handful of
+    // hardware queues, and streams beyond them share one - so a short
+    // element batch could wait behind a long trajectory launch that merely
+    // shares its queue. Two element streams (ahead in priority) and up to
+    // three program streams stay within the queues.
+    std::vector<cudaStream_t> streams;
     int queue_blocks = 0;
 
     std::mutex mu;                  // intake, completions, counters below
@@ -209,6 +219,7 @@ bool cftg_server::launch_prog(Slot &sl)
     const SeqProgram &P = *head->P;
     const size_t esz = head->esz;
     const size_t per_lane = (size_t)(P.n_scratch_out + P.reach) * esz;
+    const size_t state_lane = (size_t)P.n_scratch_out * esz;
     size_t lanes = 0;
     std::vector<Req *> take;
     for (auto it = prog_q.begin(); it != prog_q.end();) {
@@ -217,7 +228,9 @@ bool cftg_server::launch_prog(Slot &sl)
             ++it;
             continue;
         }
-        if (!take.empty() && lanes + q->r.lanes > cfg.max_batch_lanes) break;
+        if (!take.empty() && (lanes + q->r.lanes > cfg.max_batch_lanes ||
+                              (lanes + q->r.lanes) * state_lane > sl.h_init_cap))
+            break;
         take.push_back(q);
         lanes += q->r.lanes;
         it = prog_q.erase(it);
@@ -243,18 +256,23 @@ bool cftg_server::launch_prog(Slot &sl)
     const uint64_t t = now_ns();
     uint8_t *state = static_cast<uint8_t *>(base) + sl.prog_off;
     uint8_t *scratch = state + lanes * P.n_scratch_out * esz;
-    size_t l = 0;
+    // the initial blocks through the slot's pinned staging (allocated once:
+    // freeing pinned memory would wait for the whole device), so the copy is
+    // truly asynchronous on a stream other batches share
+    const size_t init_bytes = lanes * P.n_scratch_out * esz;
     cudaError_t e = cudaSuccess;
+    size_t l = 0;
     for (Req *q : take) {
         q->t_admit = t;
         sl.reqs.push_back(q);
         sl.lane0.push_back(l);
         for (size_t j = 0; j < q->r.lanes; j++) sl.h_seg[l + j] = q->r.runs;
         if (e == cudaSuccess && !q->init.empty())
-            e = cudaMemcpyAsync(state + l * P.n_scratch_out * esz, q->init.data(), q->init.size(),
-                                cudaMemcpyHostToDevice, sl.s);
+            memcpy(sl.h_init + l * P.n_scratch_out * esz, q->init.data(), q->init.size());
         l += q->r.lanes;
     }
+    if (e == cudaSuccess && init_bytes)
+        e = cudaMemcpyAsync(state, sl.h_init, init_bytes, cudaMemcpyHostToDevice, sl.s);
     std::iota(sl.h_order, sl.h_order + lanes, 0u);
     std::stable_sort(sl.h_order, sl.h_order + lanes,
                      [&](uint32_t x, uint32_t y) { return sl.h_seg[x] > sl.h_seg[y]; });
@@ -420,13 +438,13 @@ void cftg_server::loop()
 static void free_slot(Slot &sl)
 {
     if (sl.ev) cudaEventDestroy(sl.ev);
-    if (sl.s) cudaStreamDestroy(sl.s);
     for (void *p : {(void *)sl.d_calls, (void *)sl.d_prefix, (void *)sl.d_counter, (void *)sl.d_flags,
                     (void *)sl.d_seg, (void *)sl.d_order, (void *)sl.d_lstatus, (void *)sl.d_word,
                     (void *)sl.d_lflags})
         if (p) cudaFree(p);
     for (void *p : {(void *)sl.h_calls, (void *)sl.h_prefix, (void *)sl.h_flags, (void *)sl.h_seg,
-                    (void *)sl.h_order, (void *)sl.h_lstatus, (void *)sl.h_word, (void *)sl.h_lflags})
+                    (void *)sl.h_order, (void *)sl.h_lstatus, (void *)sl.h_word, (void *)sl.h_lflags,
+                    (void *)sl.h_init})
         if (p) cudaFreeHost(p);
 }
 
@@ -445,6 +463,7 @@ extern "C" void cftg_server_free(cftg_server *s)
     }
     cudaSetDevice(s->dev->ordinal);
     for (auto &sl : s->slots) free_slot(sl);
+    for (cudaStream_t st : s->streams) cudaStreamDestroy(st);
     if (s->base) cudaFree(s->base);
     for (Req *q : s->elem_q) delete q;
     for (Req *q : s->prog_q) delete q;
@@ -482,10 +501,20 @@ extern "C" cft_status cftg_server_create(cft_device *dev, const cftg_server_conf
     bool ok = cudaMalloc(&s->base, c.hbm_budget) == cudaSuccess;
     s->arena.init(c.hbm_budget);
     s->slots.resize((size_t)c.max_inflight + c.max_program_inflight);
+    const size_t ne = std::min<size_t>(2, c.max_inflight);
+    const size_t np = std::min<size_t>(3, c.max_program_inflight);
+    int lo_prio = 0, hi_prio = 0;
+    cudaDeviceGetStreamPriorityRange(&lo_prio, &hi_prio);
+    for (size_t i = 0; ok && i < ne + np; i++) {
+        cudaStream_t st = nullptr;
+        ok = cudaStreamCreateWithPriority(&st, cudaStreamNonBlocking, i < ne ? hi_prio : lo_prio) ==
+             cudaSuccess;
+        if (ok) s->streams.push_back(st);
+    }
     for (size_t i = 0; ok && i < s->slots.size(); i++) {
         Slot &sl = s->slots[i];
-        ok = cudaStreamCreateWithFlags(&sl.s, cudaStreamNonBlocking) == cudaSuccess &&
-             cudaEventCreateWithFlags(&sl.ev, cudaEventDisableTiming) == cudaSuccess;
+        sl.s = i < c.max_inflight ? s->streams[i % ne] : s->streams[ne + (i - c.max_inflight) % np];
+        ok = cudaEventCreateWithFlags(&sl.ev, cudaEventDisableTiming) == cudaSuccess;
         if (!ok) break;
         if (i < c.max_inflight) {
             const size_t k = c.max_batch_calls;
@@ -506,7 +535,9 @@ extern "C" cft_status cftg_server_create(cft_device *dev, const cftg_server_conf
                  cudaHostAlloc(&sl.h_order, l * 4, 0) == cudaSuccess &&
                  cudaHostAlloc(&sl.h_lstatus, l * 4, 0) == cudaSuccess &&
                  cudaHostAlloc(&sl.h_lflags, l, 0) == cudaSuccess &&
-                 cudaHostAlloc(&sl.h_word, 4 * sizeof(uint32_t), 0) == cudaSuccess;
+                 cudaHostAlloc(&sl.h_word, 4 * sizeof(uint32_t), 0) == cudaSuccess &&
+                 cudaHostAlloc(&sl.h_init, SERVE_INIT_STAGING, 0) == cudaSuccess;
+            sl.h_init_cap = SERVE_INIT_STAGING;
         }
     }
     if (!ok) {
@@ -575,6 +606,9 @@ extern "C" cft_status cftg_server_submit(cftg_server *s, const cftg_request *r)
         q->P = P;
         q->esz = esz_of(P->fmt);
         q->out_bytes = r->lanes * P->n_scratch_out * q->esz;
+        if (q->out_bytes > SERVE_INIT_STAGING)
+            return refuse(CFT_ERR_INVALID_ARGUMENT, "a program request's initial blocks exceed "
+                                                    "the 16 MiB a program batch stages");
         if (P->n_scratch_out) {
             if (!r->init)
                 return refuse(CFT_ERR_INVALID_ARGUMENT, "a program request needs its initial blocks");

@@ -86,20 +86,4 @@ extern "C" cft_status cft_max_mag(cft_device *, cft_format, const void *, const 
 extern "C" cft_status cft_minnum_mag(cft_device *, cft_format, const void *, const void *, void *, size_t, uint32_t *) { clear_error(); return refuse("cft_minnum_mag"); }
 extern "C" cft_status cft_maxnum_mag(cft_device *, cft_format, const void *, const void *, void *, size_t, uint32_t *) { clear_error(); return refuse("cft_maxnum_mag"); }
 
-// reductions: "next" for this backend (cft_supports answers 0 for them)
-extern "C" cft_status cft_reduce(cft_device *dev, cft_op, cft_format, cft_round, const void *, const void *,
-                                 void *, size_t, uint32_t *, uint32_t *bus_out)
-{
-    clear_error();
-    if (bus_out) *bus_out = 0;
-    if (!dev) return CFT_ERR_INVALID_ARGUMENT;
-    return refuse("cft_reduce");
-}
-extern "C" cft_status cft_reduce_seg(cft_device *dev, cft_op, cft_format, cft_round, const void *,
-                                     const void *, void *, size_t, size_t, uint32_t *, uint32_t *bus_out)
-{
-    clear_error();
-    if (bus_out) *bus_out = 0;
-    if (!dev) return CFT_ERR_INVALID_ARGUMENT;
-    return refuse("cft_reduce_seg");
-}
+

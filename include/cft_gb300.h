@@ -153,6 +153,20 @@ CFT_API void cftg_traj_group_free(cftg_traj_group *g);
 CFT_API cft_status cftg_fill_operands(int fmt, void *d_out, size_t n, uint64_t seed,
                                       int exp_range, uint32_t special_ppm, void *stream);
 
+/* ---- reductions over device memory --------------------------------------
+ *
+ * cft_reduce / cft_reduce_seg (the reference's fixed tree, compositions and
+ * 9.4 infinity rule, same bits and flags) over DEVICE operands, asynchronous
+ * on `stream`: d_out receives the n / seg results (seg = n: one result),
+ * d_flags[0] the flags (two device words, overwritten). For seg == n the
+ * tree's partial results go to d_partials, cftg_reduce_partial_bytes(fmt, n)
+ * bytes of device memory. Operands aligned to their element size (16 bytes
+ * at most). */
+CFT_API cft_status cftg_reduce_device(cft_device *dev, int op, int fmt, int rnd, const void *a,
+                                      const void *b, void *d_out, size_t n, size_t seg,
+                                      void *d_partials, uint32_t *d_flags, void *stream);
+CFT_API size_t cftg_reduce_partial_bytes(int fmt, size_t n);
+
 /* ---- a program run that allocates nothing ------------------------------
  *
  * No counterpart in the reference: an addition of this library. It exists

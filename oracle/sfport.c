@@ -14,6 +14,7 @@
  */
 #include "sfport.h"
 
+#include <stdlib.h>
 #include <string.h>
 
 /* ---- format geometry (host/src/softfloat.c:10-16) ------------------- */
@@ -1082,5 +1083,208 @@ int sfp_run(int kind, int fmt, int op, int rnd, const void *a, const void *b,
     }
     if (acc)
         *acc = all;
+    return 0;
+}
+
+/* ---- reductions ---------------------------------------------------------
+ *
+ * The fixed tree (host/src/softfloat.c:850-937): T(lo, hi) is +0 for an
+ * empty range, the leaf for one element (the element itself for SUM; the
+ * rounded product for DOT), else add(T(lo, mid), T(mid, hi)) with mid = lo
+ * + k/2, k the smallest power of two >= hi - lo - so the left child is the
+ * largest power of two strictly inside the range. The add is ADD with the
+ * left subtree in a and the right in c. Flags OR over every node.
+ *
+ * The compositions (host/src/device.c:2880-3066): SUMSQ is DOT(a, a) and
+ * SUMABS is SUM over the magnitudes; when either's result is a NaN and an
+ * element is an infinity, the result is +inf and the flags are INVALID iff
+ * an element is a signalling NaN (IEEE 754-2019 9.4), replacing the tree's.
+ * MAXALL halves with the elementwise MAX (op 8): pairs (x[i], x[i + m/2]),
+ * an odd last element carried; n == 1 returns a[0] verbatim. n == 0 gives
+ * +0 (MAXALL: -inf) and no flags (device.c:2812-2832). The segmented form
+ * is the same per slice, flags ORed (device.c:3201-3216). */
+static int red_tree(int fmt, int op, int rnd, const uint8_t *a, const uint8_t *b, size_t lo,
+                    size_t hi, uint8_t *out, uint32_t *flags)
+{
+    const size_t esz = (size_t)FMTS[fmt].width / 8;
+    uint8_t left[32], right[32], zero[32];
+    uint32_t lf = 0, rf = 0, af = 0;
+    size_t m, k, mid;
+    *flags = 0;
+    memset(zero, 0, sizeof zero);
+    if (hi == lo) {
+        memset(out, 0, esz);
+        return 0;
+    }
+    if (hi - lo == 1) {
+        if (op == 25)
+            return sfp_compute(fmt, 3, rnd, a + lo * esz, b + lo * esz, zero, out, flags);
+        memcpy(out, a + lo * esz, esz);
+        return 0;
+    }
+    m = hi - lo;
+    k = 1;
+    while (k < m)
+        k <<= 1;
+    mid = lo + (k >> 1);
+    if (red_tree(fmt, op, rnd, a, b, lo, mid, left, &lf))
+        return 1;
+    if (red_tree(fmt, op, rnd, a, b, mid, hi, right, &rf))
+        return 1;
+    if (sfp_compute(fmt, 1, rnd, left, zero, right, out, &af))
+        return 1;
+    *flags = lf | rf | af;
+    return 0;
+}
+
+static int is_nan_bytes(const fmt_t *f, const uint8_t *p)
+{
+    ob v;
+    ob_load(&v, p, f->width / 8);
+    if (ob_extract(&v, f->man_w, f->exp_w) != f->exp_mask)
+        return 0;
+    ob_mask(&v, f->man_w);
+    return !ob_is_zero(&v);
+}
+
+/* 9.4's infinity rule over a[0..n): 1 when it applies (device.c:2678-2703). */
+static int inf_override(const fmt_t *f, const uint8_t *a, size_t n, uint8_t *out,
+                        uint32_t *flags)
+{
+    const int nb = f->width / 8;
+    int saw_inf = 0, saw_snan = 0;
+    size_t i;
+    for (i = 0; i < n; i++) {
+        ob v, frac;
+        ob_load(&v, a + i * nb, nb);
+        if (ob_extract(&v, f->man_w, f->exp_w) != f->exp_mask)
+            continue;
+        frac = v;
+        ob_mask(&frac, f->man_w);
+        if (ob_is_zero(&frac))
+            saw_inf = 1;
+        else if (!ob_bit(&v, f->man_w - 1))
+            saw_snan = 1;
+    }
+    if (!saw_inf)
+        return 0;
+    {
+        ob o;
+        enc_inf(f, 0, &o);
+        ob_store(&o, out, nb);
+    }
+    *flags = saw_snan ? 1u : 0u;          /* INVALID */
+    return 1;
+}
+
+int sfp_reduce(int fmt, int op, int rnd, const void *a, const void *b, void *d, size_t n,
+               uint32_t *flags)
+{
+    const fmt_t *f;
+    size_t esz;
+    uint8_t *pd = (uint8_t *)d;
+    const uint8_t *pa = (const uint8_t *)a, *pb = (const uint8_t *)b;
+    uint32_t fl = 0;
+    if (bad_fmt(fmt) || !d)
+        return 1;
+    f = &FMTS[fmt];
+    esz = (size_t)f->width / 8;
+    *flags = 0;
+    if (n == 0) {
+        ob z;
+        if (op == 31)
+            enc_inf(f, 1, &z);
+        else
+            ob_zero(&z);
+        ob_store(&z, pd, (int)esz);
+        return 0;
+    }
+    if (op == 31) {
+        uint8_t *buf = (uint8_t *)malloc((n + 1) * esz);
+        size_t m = n, i;
+        if (!buf)
+            return 1;
+        memcpy(buf, pa, n * esz);
+        while (m > 1) {
+            const size_t h = m / 2;
+            const int odd = (m & 1u) != 0;
+            for (i = 0; i < h; i++) {
+                uint8_t t[32];
+                uint32_t pf = 0;
+                if (sfp_compute(fmt, 8, rnd, buf + i * esz, buf + (i + h) * esz, NULL, t, &pf)) {
+                    free(buf);
+                    return 1;
+                }
+                fl |= pf;
+                memcpy(buf + i * esz, t, esz);     /* i < h: reads of later pairs untouched */
+            }
+            if (odd)
+                memmove(buf + h * esz, buf + 2 * h * esz, esz);
+            m = h + (size_t)odd;
+        }
+        memcpy(pd, buf, esz);
+        free(buf);
+        *flags = fl;
+        return 0;
+    }
+    if (op == 28 || op == 29) {
+        int st;
+        if (op == 28) {
+            st = red_tree(fmt, 25, rnd, pa, pa, 0, n, pd, &fl);
+        } else {
+            uint8_t *tmp = (uint8_t *)malloc(n * esz);
+            size_t i;
+            if (!tmp)
+                return 1;
+            for (i = 0; i < n; i++) {
+                uint32_t af = 0;
+                if (sfp_compute(fmt, 4, rnd, pa + i * esz, NULL, NULL, tmp + i * esz, &af)) {
+                    free(tmp);
+                    return 1;
+                }
+                fl |= af;
+            }
+            {
+                uint32_t sf = 0;
+                st = red_tree(fmt, 24, rnd, tmp, NULL, 0, n, pd, &sf);
+                fl |= sf;
+            }
+            free(tmp);
+        }
+        if (st)
+            return 1;
+        if (is_nan_bytes(f, pd)) {
+            uint32_t of = 0;
+            if (inf_override(f, pa, n, pd, &of))
+                fl = of;
+        }
+        *flags = fl;
+        return 0;
+    }
+    if (op != 24 && op != 25)
+        return 1;
+    if (red_tree(fmt, op, rnd, pa, pb, 0, n, pd, &fl))
+        return 1;
+    *flags = fl;
+    return 0;
+}
+
+int sfp_reduce_seg(int fmt, int op, int rnd, const void *a, const void *b, void *d, size_t n,
+                   size_t seg, uint32_t *flags)
+{
+    const size_t esz = bad_fmt(fmt) ? 0 : (size_t)FMTS[fmt].width / 8;
+    size_t s;
+    uint32_t all = 0;
+    if (!esz || !seg || n % seg)
+        return 1;
+    for (s = 0; s < n / seg; s++) {
+        uint32_t fl = 0;
+        if (sfp_reduce(fmt, op, rnd, (const uint8_t *)a + s * seg * esz,
+                       b ? (const uint8_t *)b + s * seg * esz : NULL, (uint8_t *)d + s * esz,
+                       seg, &fl))
+            return 1;
+        all |= fl;
+    }
+    *flags = all;
     return 0;
 }

@@ -39,6 +39,14 @@ int sfp_sqrt(int fmt, int rnd, const uint8_t *a, uint8_t *d, uint32_t *flags);
  * r makes operand r element 0 for every i. `kind` 0 = opcode `op`,
  * 1 = division, 2 = square root. lane_flags (n bytes) may be NULL; *acc
  * receives the OR of every element's flags. Returns 0 or 1. */
+/* Reductions (opcodes 24 SUM, 25 DOT, 28 SUMSQ, 29 SUMABS, 31 MAXALL): one
+ * element into d, the reference's fixed tree and compositions; the
+ * segmented form writes n / seg results. Return 0, or 1 on a refusal. */
+int sfp_reduce(int fmt, int op, int rnd, const void *a, const void *b, void *d, size_t n,
+               uint32_t *flags);
+int sfp_reduce_seg(int fmt, int op, int rnd, const void *a, const void *b, void *d, size_t n,
+                   size_t seg, uint32_t *flags);
+
 int sfp_run(int kind, int fmt, int op, int rnd, const void *a, const void *b,
             const void *c, void *d, size_t n, uint32_t scalar_mask,
             uint8_t *lane_flags, uint32_t *acc);
