@@ -661,6 +661,28 @@ __global__ void __launch_bounds__(32) k_traj_g(const TrajLaunch L)
     }
 }
 
+// A kernel's dynamic shared-memory ceiling and L1/shared split are set once
+// a device, to the device's opt-in maximum: changing a function's attributes
+// between launches can wait for the function's running launches, which in a
+// serving loop are trajectories of a quarter second.
+template <typename K>
+static cudaError_t smem_ceiling_once(K kernel, unsigned &done_mask)
+{
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const unsigned bit = 1u << (dev & 31);
+    if (done_mask & bit) return cudaSuccess;
+    int optin = 0;
+    cudaError_t e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 cudaSharedmemCarveoutMaxShared);
+    if (e == cudaSuccess) done_mask |= bit;
+    return e;
+}
+
 template <int FMT>
 static int seq_threads(const SeqProgram &P, size_t *smem)
 {
@@ -694,11 +716,8 @@ static cudaError_t go_traj(const TrajLaunch &L, cudaStream_t s)
     const size_t scr = (size_t)L.P.reach * W * 4;
     const bool shared = L.P.reach > 0 && (regs + scr) * T <= (160u << 10);
     if (shared) smem += scr * T;
-    cudaError_t e = cudaFuncSetAttribute(k_traj<FMT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_traj<FMT>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                 cudaSharedmemCarveoutMaxShared);
+    static unsigned done = 0;
+    cudaError_t e = smem_ceiling_once(k_traj<FMT>, done);
     if (e != cudaSuccess) return e;
     const size_t blocks = (L.n + T - 1) / T;
     k_traj<FMT><<<(unsigned)blocks, T, smem, s>>>(L, shared);
@@ -711,11 +730,8 @@ static cudaError_t go_traj_g(const TrajLaunch &L, cudaStream_t s)
     constexpr int W = sf::Fmt<FMT>::W;
     const int LPB = 32 / L.G;
     const size_t smem = (size_t)L.nloc * (size_t)(W * LPB + 1) * 4;
-    cudaError_t e = cudaFuncSetAttribute(k_traj_g<FMT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_traj_g<FMT>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                 cudaSharedmemCarveoutMaxShared);
+    static unsigned done = 0;
+    cudaError_t e = smem_ceiling_once(k_traj_g<FMT>, done);
     if (e != cudaSuccess) return e;
     const size_t blocks = (L.n + LPB - 1) / LPB;
     k_traj_g<FMT><<<(unsigned)blocks, 32, smem, s>>>(L);
@@ -752,8 +768,8 @@ static cudaError_t go_seq(const SeqLaunch &L, cudaStream_t s)
     if (T > 256) T = 256;
     if (T < 32) T = 32;
     const size_t smem = per_lane * T;
-    cudaError_t e = cudaFuncSetAttribute(k_seq<FMT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
+    static unsigned done = 0;
+    cudaError_t e = smem_ceiling_once(k_seq<FMT>, done);
     if (e != cudaSuccess) return e;
     const size_t blocks = (L.n + T - 1) / T;
     k_seq<FMT><<<(unsigned)blocks, T, smem, s>>>(L, 0, L.n);
