@@ -278,6 +278,28 @@ def run_sweep(h, suites, args):
     return res
 
 
+def run_reduce(h, suites, args):
+    """The reduction suite, then the oracle over each cell's checked prefix."""
+    sys.path.insert(0, str(ROOT / "tests"))
+    import oracle_lib
+    res = suites.reduce(h, n=min(args.n, 1 << 24))
+    checks = res.pop("_checks")
+    o = oracle_lib.Oracle()
+    vp, i, sz = ctypes.c_void_p, ctypes.c_int, ctypes.c_size_t
+    o.L.sfp_reduce.argtypes = [i, i, i, vp, vp, vp, sz, ctypes.POINTER(ctypes.c_uint32)]
+    bad = 0
+    for ck in checks:
+        d = np.zeros_like(ck["d"])
+        fl = ctypes.c_uint32()
+        n = ck["a"].shape[0]
+        assert o.L.sfp_reduce(ck["fmt"], ck["op"], 0, ck["a"].ctypes.data, ck["b"].ctypes.data,
+                              d.ctypes.data, n, ctypes.byref(fl)) == 0
+        bad += int(not np.array_equal(d, ck["d"]) or fl.value != ck["flags"])
+    res["oracle_cells_checked"] = len(checks)
+    res["oracle_mismatches"] = bad
+    return res
+
+
 def dist_init():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -344,14 +366,14 @@ def main():
                     help="serving suite: fraction of requests that are program ensembles")
     ap.add_argument("--inflight", type=int, default=6,
                     help="serving suite: element batches on the device at once")
-    ap.add_argument("--program-inflight", type=int, default=6,
+    ap.add_argument("--program-inflight", type=int, default=2,
                     help="serving suite: program batches on the device at once")
     ap.add_argument("--seconds", type=float, default=60.0,
                     help="length of the serving suite's request stream")
     ap.add_argument("--fmt", type=int, default=3, help="format of the headline leg (3 = binary256)")
     ap.add_argument("--op", default="fma", choices=["fma", "add", "mul", "div", "sqrt"],
                     help="operation of the --profile leg")
-    ap.add_argument("--suite", default=None, choices=["uneven", "trajectories", "sweep", "serving"],
+    ap.add_argument("--suite", default=None, choices=["uneven", "trajectories", "sweep", "serving", "reduce"],
                     help="run one of the secondary configurations instead of the headline")
     args = ap.parse_args()
     if args.impl == "reference":
@@ -366,6 +388,8 @@ def main():
             print(json.dumps(run_trajectories(h, suites, args)))
         elif args.suite == "sweep":
             print(json.dumps(run_sweep(h, suites, args)))
+        elif args.suite == "reduce":
+            print(json.dumps(run_reduce(h, suites, args)))
         elif args.suite == "serving":
             z = np.load(ROOT / "tests" / "golden" / "odes.npz")
             print(json.dumps(suites.serving(h, z["hh_image"], z["hh_bank"], rate=args.rate,

@@ -369,7 +369,7 @@ def hh_init(lanes, seed):
 
 def serving(h, hh_image, hh_bank, rate=20000.0, seconds=60.0, seed=5, budget=40 << 30,
             program_frac=0.02, hh_lanes=32, max_log2=22, sample_every=2000, max_inflight=6,
-            max_program_inflight=6, max_batch_elements=1 << 24):
+            max_program_inflight=2, max_batch_elements=1 << 24):
     """Open-loop serving: requests arrive as a Poisson stream of `rate` a
     second for `seconds`; each is an element call (binary128 or binary256
     1:1, size log-uniform in [64, 2^max_log2], operation uniform over add,
@@ -562,3 +562,59 @@ def _traj_alone(L, prog, bank, init, lanes, runs):
     _lib.check(L.cftg_traj_result(t, ctypes.byref(fl), ctypes.byref(st), s), "cftg_traj_result")
     L.cftg_traj_free(t)
     return ts.cpu().numpy().view(np.uint32), int(np.bitwise_or.reduce(lf.cpu().numpy() & 0x1F))
+
+
+RED_OPS = (("sum", 24), ("dot", 25), ("sumsq", 28), ("sumabs", 29), ("maxall", 31))
+
+
+def reduce(h, n=1 << 24, reps=3, check_n=65536, seed=17):
+    """The reductions over n device-resident elements a format (normals with
+    exponents in [-20, 20], no specials, so the sums stay finite), timed with
+    CUDA events; the first check_n elements are reduced again and returned
+    with their operands for the oracle."""
+    import torch
+    from . import workload as wl
+    L = _lib.lib()
+    _bind(L)
+    vp = ctypes.c_void_p
+    i = ctypes.c_int
+    L.cftg_reduce_device.argtypes = [vp, i, i, i, vp, vp, vp, ctypes.c_size_t, ctypes.c_size_t,
+                                     vp, vp, vp]
+    L.cftg_reduce_partial_bytes.argtypes = [i, ctypes.c_size_t]
+    L.cftg_reduce_partial_bytes.restype = ctypes.c_size_t
+    stream = torch.cuda.current_stream()
+    s = stream.cuda_stream
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    cells, checks = [], []
+    word = torch.zeros(2, dtype=torch.int32, device="cuda")
+    for fmt in (1, 2, 3):
+        W = wl.words(fmt)
+        a = torch.empty(n * W, dtype=torch.int32, device="cuda")
+        b = torch.empty(n * W, dtype=torch.int32, device="cuda")
+        _lib.check(L.cftg_fill_operands(fmt, a.data_ptr(), n, seed + fmt, 20, 0, s), "fill")
+        _lib.check(L.cftg_fill_operands(fmt, b.data_ptr(), n, seed + 8 + fmt, 20, 0, s), "fill")
+        part = torch.empty(L.cftg_reduce_partial_bytes(fmt, n) // 4 + 8, dtype=torch.int32,
+                           device="cuda")
+        out = torch.zeros(W, dtype=torch.int32, device="cuda")
+        for name, op in RED_OPS:
+            def go(nn):
+                _lib.check(L.cftg_reduce_device(h, op, fmt, 0, a.data_ptr(), b.data_ptr(),
+                                                out.data_ptr(), nn, nn, part.data_ptr(),
+                                                word.data_ptr(), s), "cftg_reduce_device")
+            go(n)
+            torch.cuda.synchronize()
+            e0.record(stream)
+            for _ in range(reps):
+                go(n)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / reps
+            cells.append({"fmt": ("fp32", "fp64", "fp128", "fp256")[fmt], "op": name, "ms": ms,
+                          "gelem_s": n / ms / 1e6})
+            go(check_n)
+            torch.cuda.synchronize()
+            checks.append(dict(fmt=fmt, op=op, d=out.cpu().numpy().view(np.uint32).copy(),
+                               flags=int(word[0].item()) & 0x1F,
+                               a=a[:check_n * W].cpu().numpy().view(np.uint32).reshape(-1, W),
+                               b=b[:check_n * W].cpu().numpy().view(np.uint32).reshape(-1, W)))
+    return {"suite": "reduce", "elements": n, "cells": cells, "_checks": checks}

@@ -187,7 +187,14 @@ SFD void round_pack(int sign, uint32_t (&m)[N], int e, int rnd, uint32_t (&out)[
 {
     using F = Fmt<FMT>;
     constexpr int W = F::W;
-    const int L = sfw::bitlen(m);
+    // Most results keep their leading bit in the top word or the one below
+    // (sums without deep cancellation, quotients, roots): when every lane of
+    // the warp has it there, one clz.
+    const unsigned am = __activemask();
+    int L;
+    if (__all_sync(am, m[N - 1] != 0u)) L = 32 * N - __clz(m[N - 1]);
+    else if (__all_sync(am, m[N - 1] == 0u && m[N - 2] != 0u)) L = 32 * (N - 1) - __clz(m[N - 2]);
+    else L = sfw::bitlen(m);
     const int e_norm = e + L - 1;                 // exponent of the leading bit
     sfw::shl(m, 32 * N - L);                      // leading bit to the top
 
@@ -452,11 +459,41 @@ SFD void arith_rt(int op, const uint32_t (&x)[Fmt<FMT>::W], const uint32_t (&y)[
 
 // ---- exact division of significands ---------------------------------------
 
+// A two-word by one-word division by a normalised divisor d (top bit set)
+// through its precomputed reciprocal v = floor((2^64 - 1) / d) - 2^32
+// (Moller and Granlund, "Improved division by invariant integers", IEEE
+// Trans. Computers 60(2), 2011, Algorithm 4): u1 < d; returns floor((u1 *
+// 2^32 + u0) / d) and the remainder in r. One multiply and two corrections
+// in place of a 64-by-32-bit division per quotient digit.
+SFD uint32_t recip_norm(uint32_t d)
+{
+    return (uint32_t)(0xFFFFFFFFFFFFFFFFull / d - 0x100000000ull);
+}
+
+SFD uint32_t div_2by1(uint32_t u1, uint32_t u0, uint32_t d, uint32_t v, uint32_t &r)
+{
+    const uint64_t q = (uint64_t)v * u1 + (((uint64_t)u1 << 32) | u0);
+    uint32_t q1 = (uint32_t)(q >> 32) + 1u;
+    const uint32_t q0 = (uint32_t)q;
+    uint32_t rr = u0 - q1 * d;
+    if (rr > q0) {
+        q1--;
+        rr += d;
+    }
+    if (rr >= d) {
+        q1++;
+        rr -= d;
+    }
+    r = rr;
+    return q1;
+}
+
 // q (W+1 words) = floor(X * 2^(32W) / Y) and rnz = (remainder != 0), for X, Y
 // of W words with their top bits set. Base-2^32 long division (Knuth,
 // TAOCP vol. 2, 4.3.1, Algorithm D): each quotient digit is estimated from
-// the top two remainder words over Y's top word, refined against Y's second
-// word, and fixed by at most one add-back after the multiply-subtract.
+// the top two remainder words over Y's top word (by the reciprocal of that
+// word, computed once), refined against Y's second word, and fixed by at
+// most one add-back after the multiply-subtract.
 template <int W>
 SFD void divrem_top(const uint32_t (&X)[W], const uint32_t (&Y)[W], uint32_t (&q)[W + 1],
                     uint32_t &rnz)
@@ -476,6 +513,7 @@ SFD void divrem_top(const uint32_t (&X)[W], const uint32_t (&Y)[W], uint32_t (&q
         for (int i = 0; i < n; i++) u[n + i] = X[i];
         u[m + n] = 0u;
         const uint32_t vt = Y[n - 1], vs = Y[n - 2];
+        const uint32_t vinv = recip_norm(vt);
 #pragma unroll
         for (int j = m; j >= 0; j--) {
             const uint64_t num = ((uint64_t)u[j + n] << 32) | u[j + n - 1];
@@ -484,8 +522,9 @@ SFD void divrem_top(const uint32_t (&X)[W], const uint32_t (&Y)[W], uint32_t (&q
                 qhat = 0xFFFFFFFFull;
                 rhat = num - qhat * vt;
             } else {
-                qhat = num / vt;
-                rhat = num - qhat * vt;
+                uint32_t r32;
+                qhat = div_2by1(u[j + n], u[j + n - 1], vt, vinv, r32);
+                rhat = r32;
             }
             // at most two corrections make qhat exact or one too large
             for (int k = 0; k < 2; k++) {
@@ -614,6 +653,7 @@ SFD void isqrtrem(const uint32_t (&N)[2 * W], uint32_t (&S)[W], uint32_t &rnz)
         rem[1] = (uint32_t)(e >> 32);
         r[0] = d;
     }
+    const uint32_t rinv = recip_norm(r[0]);        // the estimates' divisor never changes
 #pragma unroll
     for (int i = 1; i < W; i++) {
         // rem = rem * B^2 + the next two words of N  (rem < (2r + 1) B^2)
@@ -625,11 +665,11 @@ SFD void isqrtrem(const uint32_t (&N)[2 * W], uint32_t (&S)[W], uint32_t &rnz)
         // top two words of rem >> 1 over r's top word (r[i-1] >= 2^31)
         const uint32_t u1 = __funnelshift_r(rem[i + 1], rem[i + 2], 1);
         const uint32_t u0 = __funnelshift_r(rem[i], rem[i + 1], 1);
-        const uint32_t rt = r[i - 1];
+        const uint32_t rt = r[i - 1];             // the first digit, every step
         uint32_t d = 0xFFFFFFFFu;
         if (u1 < rt) {
-            const uint64_t qq = (((uint64_t)u1 << 32) | u0) / rt;
-            d = qq > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)qq;
+            uint32_t rr;
+            d = div_2by1(u1, u0, rt, rinv, rr);
         }
         // D = 2 r B + d (words: d, then 2r)
         uint32_t D[RW];
