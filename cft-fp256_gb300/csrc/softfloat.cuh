@@ -349,13 +349,18 @@ SFD void fma_general(const Unp<FMT> &ua, const Unp<FMT> &ub, const Unp<FMT> &uc,
             cy = (uint32_t)(t >> 32);
         }
         const bool neg = sub && !cy;               // Y < X: the result is X - Y
-        const uint32_t m2 = neg ? 0xFFFFFFFFu : 0u;
-        uint32_t c2 = neg ? 1u : 0u;
+        // the negation only where some lane of the warp needs it (the
+        // smaller-exponent term is the larger magnitude only under deep
+        // cancellation)
+        if (__any_sync(__activemask(), neg)) {
+            const uint32_t m2 = neg ? 0xFFFFFFFFu : 0u;
+            uint32_t c2 = neg ? 1u : 0u;
 #pragma unroll
-        for (int i = 0; i < N; i++) {
-            const uint64_t t = (uint64_t)(P[i] ^ m2) + c2;
-            P[i] = (uint32_t)t;
-            c2 = (uint32_t)(t >> 32);
+            for (int i = 0; i < N; i++) {
+                const uint64_t t = (uint64_t)(P[i] ^ m2) + c2;
+                P[i] = (uint32_t)t;
+                c2 = (uint32_t)(t >> 32);
+            }
         }
         rs = neg ? s_small : s_big;
         if (sub && sfw::is_zero(P)) {              // exact cancellation
