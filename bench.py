@@ -300,6 +300,18 @@ def run_reduce(h, suites, args):
     return res
 
 
+def slowest(seconds, ws, device="cuda"):
+    """The whole job's time: the slowest rank's (an all-reduce MAX over the
+    ranks; the path shards by element and exchanges nothing else)."""
+    if ws <= 1:
+        return seconds
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(seconds)], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def dist_init():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -373,7 +385,7 @@ def main():
     ap.add_argument("--fmt", type=int, default=3, help="format of the headline leg (3 = binary256)")
     ap.add_argument("--op", default="fma", choices=["fma", "add", "mul", "div", "sqrt"],
                     help="operation of the --profile leg")
-    ap.add_argument("--suite", default=None, choices=["uneven", "trajectories", "sweep", "serving", "reduce"],
+    ap.add_argument("--suite", default=None, choices=["uneven", "trajectories", "sweep", "serving", "reduce", "link"],
                     help="run one of the secondary configurations instead of the headline")
     args = ap.parse_args()
     if args.impl == "reference":
@@ -458,10 +470,7 @@ def main():
                           "gelem_s": n * args.steps / (ms / 1e3) / 1e9}))
         cftgb.close_device(h)
         return
-    if ws > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = slowest(ms, ws)
     sec = ms / 1e3
     value = ws * n * args.steps / sec / 1e9
     per_launch = sec / args.steps
@@ -509,11 +518,7 @@ def main():
         st = L.cft_run(h, 0, fmt, 0, ha.data_ptr(), hb.data_ptr(), hc.data_ptr(), hd.data_ptr(),
                        n, ctypes.byref(fl), None)
         cftgb._lib.check(st, "cft_run")
-    e2e_sec = time.perf_counter() - t0
-    if ws > 1:
-        t = torch.tensor([e2e_sec], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_sec = float(t.item())
+    e2e_sec = slowest(time.perf_counter() - t0, ws)
     e2e_value = ws * n * e2e_steps / e2e_sec / 1e9
     e2e_ok = bool(np.array_equal(hd[:4096].numpy().view(np.uint32),
                                  td[:4096].cpu().numpy().view(np.uint32)))

@@ -618,3 +618,52 @@ def reduce(h, n=1 << 24, reps=3, check_n=65536, seed=17):
                                a=a[:check_n * W].cpu().numpy().view(np.uint32).reshape(-1, W),
                                b=b[:check_n * W].cpu().numpy().view(np.uint32).reshape(-1, W)))
     return {"suite": "reduce", "elements": n, "cells": cells, "_checks": checks}
+
+
+def link(h, nbytes=1 << 30, reps=3):
+    """The host link's rates: copy-engine copies of pinned memory each way
+    and both ways at once (torch), and this library's kernel reading and
+    writing pinned host memory in place - a binary64 NEG through cft_run
+    (reads 8 bytes and writes 8 an element, almost no arithmetic)."""
+    import torch
+    L = _lib.lib()
+    out = {}
+    hp = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+    hq = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+    hp.fill_(1)
+    dv = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    dw = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    s1, s2 = torch.cuda.Stream(), torch.cuda.Stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / 1e3 / reps
+
+    out["h2d_gbs"] = nbytes / timed(lambda: dv.copy_(hp, non_blocking=True)) / 1e9
+    out["d2h_gbs"] = nbytes / timed(lambda: hq.copy_(dv, non_blocking=True)) / 1e9
+
+    def both():
+        with torch.cuda.stream(s1):
+            dv.copy_(hp, non_blocking=True)
+        with torch.cuda.stream(s2):
+            hq.copy_(dw, non_blocking=True)
+        torch.cuda.current_stream().wait_stream(s1)
+        torch.cuda.current_stream().wait_stream(s2)
+    out["both_ways_gbs_each"] = nbytes / timed(both) / 1e9
+    n = nbytes // 8
+    fl = ctypes.c_uint32()
+
+    def neg():
+        _lib.check(L.cft_run(h, 5, 1, 0, hp.data_ptr(), None, None, hq.data_ptr(), n,
+                             ctypes.byref(fl), None), "cft_run")
+    t = timed(neg)
+    out["kernel_in_place_read_gbs"] = nbytes / t / 1e9
+    out["kernel_in_place_write_gbs"] = nbytes / t / 1e9
+    return {"suite": "link", "bytes": nbytes, **out}
