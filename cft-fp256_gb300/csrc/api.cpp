@@ -318,11 +318,12 @@ extern "C" void cft_close(cft_device *dev)
 }
 
 // Sequencer features this executor implements (reference cft.h:785-1030):
-// everything the software backend publishes except augmented addition,
-// which this backend does not carry; the segmented reductions included.
+// everything the software backend publishes, augmented addition and the
+// segmented reductions included.
 static const uint32_t SEQ_FEATURES =
     CFT_SEQ_FEAT_WIDE_CONST | CFT_SEQ_FEAT_REGS32 | CFT_SEQ_FEAT_BANK_PTR | CFT_SEQ_FEAT_KX9 |
     CFT_ALU_EXT_IMUL | CFT_SEQ_FEAT_SCRATCH | CFT_SEQ_FEAT_SCRATCH_IO | CFT_FEAT_REDUCE_SEG |
+    CFT_SEQ_FEAT_AUGADD |
     CFT_SEQ_FEAT_SCRATCH_STRICT | CFT_SEQ_FEAT_SCALAR | CFT_SEQ_FEAT_INDEXED |
     CFT_SEQ_FEAT_LANE_MASK | CFT_SEQ_FEAT_SCRATCH_STEP | CFT_SEQ_FEAT_LANE_FLAGS |
     CFT_SEQ_FEAT_FLAG_CONTROL;

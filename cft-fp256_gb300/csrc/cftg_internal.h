@@ -39,6 +39,13 @@ cudaError_t launch_elem(const ElemLaunch &L, cudaStream_t stream);
 // The kernels' dimensions for a given launch (used by the queue autotuner).
 int sm_count();
 
+// ---- augmented operations (aug.cu) ----------------------------------------
+
+// r[i], e[i] = 9.5's augmented operation fn (0 add, 1 sub, 2 mul) of a[i],
+// b[i]; *word |= the flags. Device pointers, element-aligned words.
+cudaError_t launch_aug(int fmt, int fn, const void *a, const void *b, void *r, void *e, size_t n,
+                       uint32_t *word, cudaStream_t s);
+
 // ---- reductions (reduce.cu) -------------------------------------------------
 
 enum RedMode : int { RED_SUM = 0, RED_DOT = 1, RED_SQ = 2, RED_ABS = 3, RED_MAX = 4 };

@@ -4,10 +4,8 @@
 // Accept/refuse behaviour follows the reference's cft_program_load
 // (host/src/program.c:1283-1580) rule for rule and in its order, with the
 // same status codes; the sentences are this library's own. This device
-// publishes every sequencer feature the reference's software backend does
-// except augmented addition (control codes 10 and 11), which the loader
-// therefore refuses by name, as the reference refuses it on a device
-// without CFT_SEQ_FEAT_AUGADD.
+// publishes every sequencer feature the reference's software backend does,
+// augmented addition (control codes 10 and 11) included.
 #include <cstring>
 #include <new>
 #include <vector>
@@ -346,20 +344,10 @@ cft_status validate(const std::vector<uint64_t> &ins, uint32_t n_consts, uint32_
 }
 
 // What only a device can refuse of the instructions (reference
-// program.c:925-1080): here, augmented addition, which this backend does
-// not carry. Every other feature is published.
-cft_status against_device(const std::vector<uint64_t> &ins)
+// program.c:925-1080): nothing here - this device publishes every feature
+// the software backend does.
+cft_status against_device(const std::vector<uint64_t> &)
 {
-    for (uint32_t pc = 0; pc < ins.size(); pc++) {
-        const Dec d = decode(ins[pc]);
-        if (d.ctrl && (d.op == AUGADD || d.op == AUGERR)) {
-            set_error("instruction %u is %s - 754-2019 9.5's augmentedAddition - and this device "
-                      "does not publish it (cft_caps.seq_features bit 15, CFT_SEQ_FEAT_AUGADD, "
-                      "is clear)",
-                      pc, CTRL[d.op].name);
-            return CFT_ERR_UNSUPPORTED;
-        }
-    }
     return CFT_OK;
 }
 

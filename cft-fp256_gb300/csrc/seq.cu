@@ -17,6 +17,7 @@
 // accesses to one register hit 32 consecutive banks. Only the registers
 // the program names are allocated. Scratch slots live in global memory in
 // the same structure-of-words layout across the launch's lanes.
+#include "aug.cuh"
 #include "cftg_internal.h"
 #include "simple_ops.cuh"
 
@@ -290,6 +291,23 @@ SFD void interpret(const SeqProgram &P, const Lane<sf::Fmt<FMT>::W> &R,
             pc++;
             break;
         }
+        case 10: case 11:                                    // AUGADD, AUGERR
+            // 9.5's augmentedAddition(ra, rb): r (AUGADD) or e (AUGERR) to
+            // rd, both operands read before rd is written (reference
+            // seq_exec.h:337-371); flags as an ALU instruction's
+            if (active) {
+                uint32_t xa[W], xb[W], vr[W], ve[W], fl = 0u;
+                R.get(reg5(d.ra, d.imm, 1), xa);
+                R.get(reg5(d.rb, d.imm, 2), xb);
+                sf::augmented<FMT>(sf::AUG_ADD, xa, xb, vr, ve, fl);
+                R.put(reg5(d.rd, d.imm, 0), d.op == 11 ? ve : vr);
+                if (!qd) {
+                    flags |= fl;
+                    lflag |= (uint8_t)fl;
+                }
+            }
+            pc++;
+            break;
         case 12:                                             // QUIET
             qd++;
             pc++;

@@ -31,6 +31,10 @@ constexpr uint32_t F_INVALID = 1u, F_DIVZERO = 2u, F_OVERFLOW = 4u, F_UNDERFLOW 
                    F_INEXACT = 16u;
 // Rounding attributes (host/src/softfloat.h:57-62)
 constexpr int RNE = 0, RTZ = 1, RDN = 2, RUP = 3, RMM = 4;
+// IEEE 754-2019 9.5's roundTiesTowardZero: an internal direction of the
+// augmented operations only (nearest, ties to the smaller magnitude,
+// overflow to infinity), never a caller's attribute.
+constexpr int RTTZ = 5;
 
 // Format geometry (host/src/softfloat.c:10-16). W = 32-bit words an element.
 template <int FMT> struct Fmt;
@@ -151,6 +155,7 @@ SFD bool round_up(int rnd, int sign, bool guard, bool sticky, bool lsb)
     case RTZ: return false;
     case RDN: return sign && (guard || sticky);
     case RUP: return !sign && (guard || sticky);
+    case RTTZ: return guard && sticky;
     default:  return guard;                                   // RMM
     }
 }

@@ -55,9 +55,6 @@ extern "C" cft_status cft_powr(cft_device *, cft_format, cft_round, const void *
 extern "C" cft_status cft_pown(cft_device *, cft_format, cft_round, const void *, const int64_t *, void *, size_t, uint32_t *) { clear_error(); return refuse("cft_pown"); }
 extern "C" cft_status cft_compound(cft_device *, cft_format, cft_round, const void *, const int64_t *, void *, size_t, uint32_t *) { clear_error(); return refuse("cft_compound"); }
 extern "C" cft_status cft_rootn(cft_device *, cft_format, cft_round, const void *, const int64_t *, void *, size_t, uint32_t *) { clear_error(); return refuse("cft_rootn"); }
-extern "C" cft_status cft_augmented_add(cft_device *, cft_format, const void *, const void *, void *, void *, size_t, uint32_t *) { clear_error(); return refuse("cft_augmented_add"); }
-extern "C" cft_status cft_augmented_sub(cft_device *, cft_format, const void *, const void *, void *, void *, size_t, uint32_t *) { clear_error(); return refuse("cft_augmented_sub"); }
-extern "C" cft_status cft_augmented_mul(cft_device *, cft_format, const void *, const void *, void *, void *, size_t, uint32_t *) { clear_error(); return refuse("cft_augmented_mul"); }
 extern "C" cft_status cft_scaled_prod(cft_device *, cft_format, cft_round, const void *, void *, int64_t *, size_t, uint32_t *) { clear_error(); return refuse("cft_scaled_prod"); }
 extern "C" cft_status cft_scaled_prod_sum(cft_device *, cft_format, cft_round, const void *, const void *, void *, int64_t *, size_t, uint32_t *) { clear_error(); return refuse("cft_scaled_prod_sum"); }
 extern "C" cft_status cft_scaled_prod_diff(cft_device *, cft_format, cft_round, const void *, const void *, void *, int64_t *, size_t, uint32_t *) { clear_error(); return refuse("cft_scaled_prod_diff"); }

@@ -200,6 +200,20 @@ CFT_API cft_status cft_reduce_seg(cft_device *dev, cft_op op, cft_format fmt, cf
                                   const void *a, const void *b, void *d, size_t n, size_t seg,
                                   uint32_t *flags_out, uint32_t *bus_out);
 
+/* ---- augmented arithmetic, IEEE 754-2019 9.5 (cft.h:2351-2451) -------- *
+ * r = x op y rounded with roundTiesTowardZero, e = the residual; no
+ * rounding attribute (9.5 fixes it). r and e may alias a or b but not each
+ * other. */
+CFT_API cft_status cft_augmented_add(cft_device *dev, cft_format fmt, const void *a,
+                                     const void *b, void *r, void *e, size_t n,
+                                     uint32_t *flags_out);
+CFT_API cft_status cft_augmented_sub(cft_device *dev, cft_format fmt, const void *a,
+                                     const void *b, void *r, void *e, size_t n,
+                                     uint32_t *flags_out);
+CFT_API cft_status cft_augmented_mul(cft_device *dev, cft_format fmt, const void *a,
+                                     const void *b, void *r, void *e, size_t n,
+                                     uint32_t *flags_out);
+
 /* ---- resident buffers (cft.h:2470-2705) ------------------------------- *
  * cft_alloc gives a pinned host mirror (the pointer callers use) and a
  * device copy. A run that names a pointer inside a buffer reads the device

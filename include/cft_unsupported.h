@@ -59,10 +59,6 @@ CFT_API cft_status cft_powr(cft_device *dev, cft_format fmt, cft_round rnd, cons
 CFT_API cft_status cft_pown(cft_device *dev, cft_format fmt, cft_round rnd, const void *a, const int64_t *nexp, void *d, size_t count, uint32_t *flags_out);
 CFT_API cft_status cft_compound(cft_device *dev, cft_format fmt, cft_round rnd, const void *a, const int64_t *nexp, void *d, size_t count, uint32_t *flags_out);
 CFT_API cft_status cft_rootn(cft_device *dev, cft_format fmt, cft_round rnd, const void *a, const int64_t *nexp, void *d, size_t count, uint32_t *flags_out);
-/* augmented arithmetic, 754-2019 9.5 (cft.h:2440-2451) */
-CFT_API cft_status cft_augmented_add(cft_device *dev, cft_format fmt, const void *a, const void *b, void *r, void *e, size_t n, uint32_t *flags_out);
-CFT_API cft_status cft_augmented_sub(cft_device *dev, cft_format fmt, const void *a, const void *b, void *r, void *e, size_t n, uint32_t *flags_out);
-CFT_API cft_status cft_augmented_mul(cft_device *dev, cft_format fmt, const void *a, const void *b, void *r, void *e, size_t n, uint32_t *flags_out);
 /* scaled products, 754-2019 9.4 (cft.h:2335-2347) */
 CFT_API cft_status cft_scaled_prod(cft_device *dev, cft_format fmt, cft_round rnd, const void *a, void *pr, int64_t *scale_out, size_t n, uint32_t *flags_out);
 CFT_API cft_status cft_scaled_prod_sum(cft_device *dev, cft_format fmt, cft_round rnd, const void *a, const void *b, void *pr, int64_t *scale_out, size_t n, uint32_t *flags_out);

@@ -8,9 +8,8 @@
  * nothing and the early exit only skips iterations in which no lane is
  * active.
  *
- * Not restated: augmentedAddition (control codes 10 and 11). An image
- * that uses them makes sfp_seq_run return 3; the shipped library does not
- * publish that feature either.
+ * augmentedAddition (control codes 10 and 11) runs through sfport.c's
+ * sfp_aug, the restatement of 9.5 the elementwise checks pin.
  */
 #include "sfport.h"
 
@@ -259,7 +258,21 @@ static int run_lane(const prog_t *P, const uint8_t *konst, uint8_t *regs,
             break;
         }
         case 10: case 11:                       /* AUGADD, AUGERR */
-            return 3;
+            /* 9.5's augmentedAddition(ra, rb): r or e to rd, flags as an
+             * ALU instruction's (seq_exec.h:337-371) */
+            if (active) {
+                uint8_t r[32], e[32];
+                uint32_t fl = 0;
+                if (sfp_aug(P->fmt, 0, regs + d.ra * esz, regs + d.rb * esz, r, e, &fl))
+                    return 1;
+                memcpy(regs + d.rd * esz, d.op == 11 ? e : r, esz);
+                if (!qd) {
+                    *flags |= fl;
+                    *lflag |= (uint8_t)fl;
+                }
+            }
+            pc++;
+            break;
         case 12:                                /* QUIET */
             qd++;
             pc++;

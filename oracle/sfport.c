@@ -412,6 +412,9 @@ static void unpack(const fmt_t *f, const ob *x, unp *u)
 
 /* ---- rounding (softfloat.c:120-261) --------------------------------- */
 
+/* rnd 5 is 9.5's roundTiesTowardZero, an internal direction of the
+ * augmented operations only (augmented.c; golden softfloat RND_RTTZ):
+ * nearest, ties toward the smaller magnitude, overflow to infinity. */
 static int round_up(int rnd, int sign, int guard, int sticky, int lsb)
 {
     switch (rnd) {
@@ -419,6 +422,7 @@ static int round_up(int rnd, int sign, int guard, int sticky, int lsb)
     case 4: return guard;                              /* RMM */
     case 1: return 0;                                  /* RTZ */
     case 2: return sign && (guard || sticky);          /* RDN */
+    case 5: return guard && sticky;                    /* RTTZ */
     default: return !sign && (guard || sticky);        /* RUP */
     }
 }
@@ -1286,5 +1290,172 @@ int sfp_reduce_seg(int fmt, int op, int rnd, const void *a, const void *b, void 
         all |= fl;
     }
     *flags = all;
+    return 0;
+}
+
+
+/* ---- the augmented operations, IEEE 754-2019 9.5 --------------------------
+ *
+ * (python/cft_golden/augmented.py defines them; host/src/augmented.c is its
+ * C port.) r is x op y rounded with roundTiesTowardZero, e the exact
+ * residual x op y - r, representable for addition whenever r is finite;
+ * for multiplication a residual with digits below the smallest quantum is
+ * delivered rounded the same way, with UNDERFLOW and INEXACT. Flags: an
+ * overflowing r gives (inf, inf, OVERFLOW|INEXACT); otherwise UNDERFLOW iff
+ * the residual is non-zero and below 2^emin; nothing else. An exactly zero
+ * residual takes r's sign. NaN inputs give the canonical quiet NaN twice,
+ * INVALID iff one is signalling; inf - inf and inf * 0 give it with
+ * INVALID. Addition aligns exactly only when the value exponents are
+ * within p + 1 (augmented.c's FAR bound): farther apart, r is the larger
+ * operand and e the smaller, exactly. fn: 0 add, 1 sub, 2 mul. */
+static int aug_pair(const fmt_t *f, int sign_t, const ob *t, int e0, int is_mul, ob *r,
+                    ob *e, uint32_t *flags)
+{
+    uint32_t rf = 0, ef = 0;
+    unp ur;
+    ob rm, A, B, mag;
+    int re, q, sign_e, tiny;
+    if (round_pack(f, sign_t, t, e0, 0, 5, r, &rf))
+        return 1;
+    if (rf & 4u) {
+        enc_inf(f, sign_t, r);
+        *e = *r;
+        *flags = 4u | 16u;
+        return 0;
+    }
+    unpack(f, r, &ur);
+    if (ur.kind == K_ZERO) {
+        ob_zero(&rm);
+        re = e0;
+    } else {
+        rm = ur.m;
+        re = ur.e;
+    }
+    q = e0 < re ? e0 : re;
+    if (ob_shl(&A, t, e0 - q) || ob_shl(&B, &rm, re - q))
+        return 1;
+    if (sign_t == ur.sign || ur.kind == K_ZERO) {
+        if (ob_cmp(&A, &B) >= 0) {
+            ob_sub(&mag, &A, &B);
+            sign_e = sign_t;
+        } else {
+            ob_sub(&mag, &B, &A);
+            sign_e = !sign_t;
+        }
+    } else {
+        if (ob_add(&mag, &A, &B))
+            return 1;
+        sign_e = sign_t;
+    }
+    if (ob_is_zero(&mag)) {
+        enc_zero(f, ur.sign, e);
+        *flags = 0;
+        return 0;
+    }
+    tiny = (q + ob_bitlen(&mag) - 1) < f->emin;
+    if (round_pack(f, sign_e, &mag, q, 0, 5, e, &ef))
+        return 1;
+    if (!is_mul) {
+        if (ef & 16u)
+            return 1;                         /* representable by 9.5; never */
+        *flags = tiny ? 8u : 0u;
+        return 0;
+    }
+    *flags = (ef & 16u) ? (8u | 16u) : (tiny ? 8u : 0u);
+    return 0;
+}
+
+int sfp_aug(int fmt, int fn, const uint8_t *x, const uint8_t *y, uint8_t *r, uint8_t *e,
+            uint32_t *flags)
+{
+    const fmt_t *f;
+    ob X, Y, R, E;
+    unp ua, ub;
+    int nb;
+    if (bad_fmt(fmt) || fn < 0 || fn > 2)
+        return 1;
+    f = &FMTS[fmt];
+    nb = f->width / 8;
+    ob_load(&X, x, nb);
+    ob_load(&Y, y, nb);
+    if (fn == 1) {                               /* x - y is x + (-y) */
+        if (ob_bit(&Y, f->width - 1))
+            ob_clearbit(&Y, f->width - 1);
+        else
+            ob_setbit(&Y, f->width - 1);
+    }
+    unpack(f, &X, &ua);
+    unpack(f, &Y, &ub);
+    *flags = 0;
+    if (ua.kind == K_NAN || ub.kind == K_NAN) {
+        enc_qnan(f, &R);
+        E = R;
+        *flags = ((ua.kind == K_NAN && ua.signaling) || (ub.kind == K_NAN && ub.signaling)) ? 1u : 0u;
+    } else if (fn == 2) {
+        const int sp = ua.sign ^ ub.sign;
+        if ((ua.kind == K_INF && ub.kind == K_ZERO) || (ua.kind == K_ZERO && ub.kind == K_INF)) {
+            enc_qnan(f, &R);
+            E = R;
+            *flags = 1u;
+        } else if (ua.kind == K_INF || ub.kind == K_INF) {
+            enc_inf(f, sp, &R);
+            E = R;
+        } else if (ua.kind == K_ZERO || ub.kind == K_ZERO) {
+            enc_zero(f, sp, &R);
+            E = R;
+        } else {
+            ob t;
+            if (ob_mul(&t, &ua.m, &ub.m) || aug_pair(f, sp, &t, ua.e + ub.e, 1, &R, &E, flags))
+                return 1;
+        }
+    } else if (ua.kind == K_INF && ub.kind == K_INF && ua.sign != ub.sign) {
+        enc_qnan(f, &R);
+        E = R;
+        *flags = 1u;
+    } else if (ua.kind == K_INF || ub.kind == K_INF) {
+        enc_inf(f, ua.kind == K_INF ? ua.sign : ub.sign, &R);
+        E = R;
+    } else if (ua.kind == K_ZERO && ub.kind == K_ZERO) {
+        enc_zero(f, ua.sign == ub.sign ? ua.sign : 0, &R);
+        E = R;
+    } else if (ua.kind == K_ZERO || ub.kind == K_ZERO) {
+        R = ua.kind == K_ZERO ? Y : X;
+        enc_zero(f, ob_bit(&R, f->width - 1), &E);
+    } else {
+        const int vx = ua.e + ob_bitlen(&ua.m) - 1, vy = ub.e + ob_bitlen(&ub.m) - 1;
+        const int gap = vx > vy ? vx - vy : vy - vx;
+        if (gap >= f->prec + 2) {
+            /* FAR: the larger operand is r, the smaller e, exactly */
+            const int xbig = vx > vy;
+            R = xbig ? X : Y;
+            E = xbig ? Y : X;
+            *flags = ((xbig ? vy : vx) < f->emin) ? 8u : 0u;
+        } else {
+            const int e0 = ua.e < ub.e ? ua.e : ub.e;
+            ob A, B, t;
+            int st;
+            if (ob_shl(&A, &ua.m, ua.e - e0) || ob_shl(&B, &ub.m, ub.e - e0))
+                return 1;
+            if (ua.sign == ub.sign) {
+                if (ob_add(&t, &A, &B))
+                    return 1;
+                st = ua.sign;
+            } else if (ob_cmp(&A, &B) >= 0) {
+                ob_sub(&t, &A, &B);
+                st = ua.sign;
+            } else {
+                ob_sub(&t, &B, &A);
+                st = ub.sign;
+            }
+            if (ob_is_zero(&t)) {
+                enc_zero(f, 0, &R);               /* exact cancellation */
+                E = R;
+            } else if (aug_pair(f, st, &t, e0, 0, &R, &E, flags)) {
+                return 1;
+            }
+        }
+    }
+    ob_store(&R, r, nb);
+    ob_store(&E, e, nb);
     return 0;
 }

@@ -47,6 +47,12 @@ int sfp_reduce(int fmt, int op, int rnd, const void *a, const void *b, void *d, 
 int sfp_reduce_seg(int fmt, int op, int rnd, const void *a, const void *b, void *d, size_t n,
                    size_t seg, uint32_t *flags);
 
+/* IEEE 754-2019 9.5's augmented operations on one element pair: fn 0
+ * augmentedAddition, 1 augmentedSubtraction, 2 augmentedMultiplication;
+ * r and e receive the rounded result and the residual. */
+int sfp_aug(int fmt, int fn, const uint8_t *x, const uint8_t *y, uint8_t *r, uint8_t *e,
+            uint32_t *flags);
+
 int sfp_run(int kind, int fmt, int op, int rnd, const void *a, const void *b,
             const void *c, void *d, size_t n, uint32_t scalar_mask,
             uint8_t *lane_flags, uint32_t *acc);

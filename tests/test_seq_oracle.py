@@ -17,8 +17,6 @@ CASES = su.cases()
 @pytest.mark.parametrize("path", CASES, ids=[p.stem for p in CASES])
 def test_oracle_executor_matches_reference_outputs(oracle, path):
     case = su.load(path)
-    if su.uses_augadd(case["image"]):
-        pytest.skip("augmented addition is outside this oracle and this backend")
     got = su.run_oracle(oracle, case)
     assert got is not None
     assert su.compare(got, case) == []
@@ -62,8 +60,6 @@ def test_loader_decisions_match_the_reference():
         off += n
         buf = img if n else np.zeros(1, np.uint8)
         got = L.cftg_program_check(buf.ctypes.data, int(n), 256)
-        if want == 0 and su.uses_augadd(img):
-            want = 2            # this device does not publish CFT_SEQ_FEAT_AUGADD
         if got != want:
             bad.append((i, int(want), got, L.cft_last_error()))
     assert not bad, f"{len(bad)} of {len(z['lens'])} differ, first {bad[:4]}"
