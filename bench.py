@@ -43,6 +43,10 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT / "cft-fp256_gb300"))
 
 METRIC = "fp256/fp128 FMA Gelem/s bit-exact (plain vs batched); mixed-load p50/p99 latency"
+# GPU reads of pinned host memory, GB/s, on this machine's GB300 hosts (the
+# copy engines' host-to-device rate and a streaming kernel's, which agree;
+# bench.py --suite link measures it)
+LINK_READ_GBS = 211.0
 # DRAM bytes (read + write) an element of the FMA kernel, from the ncu
 # capture summarised in profiles/k_elem_fma256_n4M.md (518.3 MB / 4,194,304)
 TRAFFIC_B_PER_ELEM = {3: 518.3e6 / 4194304}
@@ -539,9 +543,14 @@ def main():
                                    "normals exp in [-64,64], 10% specials, cancellation triples)",
                        "elements_per_gpu": n, "l2": "inputs 1.5 GiB > L2, no flush",
                        "parallelism": f"replicas x{ws} (element shards)"},
-            "e2e": {"value": e2e_value, "unit": "Gelem/s", "h2d_bytes_per_step": 3 * 32 * n,
-                    "d2h_bytes_per_step": 32 * n + 8, "path": "cft_run, pinned host buffers",
-                    "steps": e2e_steps},
+            "e2e": {"value": e2e_value, "unit": "Gelem/s", "h2d_bytes_per_step": 3 * 4 * W * n,
+                    "d2h_bytes_per_step": 4 * W * n + 8, "path": "cft_run, pinned host buffers",
+                    "steps": e2e_steps,
+                    "link_bound_gelem_s": LINK_READ_GBS / (3 * 4 * W),
+                    "link_note": f"the kernel reads the operands in host memory in place; GPU "
+                                 f"reads of pinned host memory top out at {LINK_READ_GBS:.0f} GB/s "
+                                 f"on this host (bench.py --suite link), so e2e is bound at "
+                                 f"{LINK_READ_GBS / (3 * 4 * W):.2f} Gelem/s"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                          "frac": achieved / hbm_peak,
                          "traffic": (TRAFFIC_B_PER_ELEM[fmt] * n) if fmt in TRAFFIC_B_PER_ELEM else None,
