@@ -103,13 +103,16 @@ __global__ void __launch_bounds__(256) k_queue(const QCall *__restrict__ calls,
                                                const QTile *__restrict__ tiles, uint32_t ntiles,
                                                uint32_t *counter, uint32_t *call_flags)
 {
+    // the next tile's index is taken while this one is computed, so the
+    // counter's round trip is hidden behind the work
     __shared__ uint32_t next;
+    if (threadIdx.x == 0) next = atomicAdd(counter, 1u);
     for (;;) {
-        if (threadIdx.x == 0) next = atomicAdd(counter, 1u);
         __syncthreads();
         const uint32_t t = next;
         __syncthreads();
         if (t >= ntiles) break;
+        if (threadIdx.x == 0) next = atomicAdd(counter, 1u);
         const QTile tl = tiles[t];
         const QCall c = calls[tl.call];
         uint32_t acc;

@@ -168,7 +168,16 @@ SFD void cta_perfect(const void *a, const void *b, size_t base, uint32_t count, 
 #pragma unroll
         for (int w = 0; w < W; w++) v[w] = vals[0][w];
     }
-    for (uint32_t s = 1; s < P; s <<= 1) {
+    // the levels inside a warp by shuffles (no block barrier), the rest
+    // through shared memory
+    const uint32_t Pw = P < 32u ? P : 32u;
+    for (uint32_t s = 1; s < Pw; s <<= 1) {
+        uint32_t r[W];
+#pragma unroll
+        for (int w = 0; w < W; w++) r[w] = __shfl_down_sync(0xFFFFFFFFu, v[w], s);
+        if (have && (t & (2 * s - 1)) == 0) comb<FMT, MODE>(v, r, rnd, fl);
+    }
+    for (uint32_t s = 32; s < P; s <<= 1) {
         __syncthreads();
         if (have && (t & (2 * s - 1)) == s) {
 #pragma unroll

@@ -524,8 +524,16 @@ SFD void divrem_top(const uint32_t (&X)[W], const uint32_t (&Y)[W], uint32_t (&q
         u[m + n] = 0u;
         const uint32_t vt = Y[n - 1], vs = Y[n - 2];
         const uint32_t vinv = recip_norm(vt);
+        // the top digit is 0 or 1 (X < 2Y): X >= Y, and subtract Y if so
+        {
+            uint32_t d[n];
+            const uint32_t br = sfw::sub(d, X, Y);
+            q[m] = br ? 0u : 1u;
 #pragma unroll
-        for (int j = m; j >= 0; j--) {
+            for (int i = 0; i < n; i++) u[m + i] = br ? u[m + i] : d[i];
+        }
+#pragma unroll
+        for (int j = m - 1; j >= 0; j--) {
             const uint64_t num = ((uint64_t)u[j + n] << 32) | u[j + n - 1];
             uint64_t qhat, rhat;
             if (u[j + n] >= vt) {

@@ -120,3 +120,18 @@ def test_program_info_and_digest(gpu):
     assert st == 0
     assert bytes(out) == hashlib.sha256(img.tobytes() + bank.tobytes()).digest()
     L.cft_program_free(prog)
+
+
+@pytest.mark.parametrize("cert", CERTS)
+def test_certificate_segment_lines(gpu, cert):
+    """The GPU run writes the certificate's own segment lines (start and end
+    state hashes, flags, STATUS) for the reference's fp256 certificates."""
+    from cftgb import certify
+    z = np.load(su.GOLD / f"{cert}_cert.npz")
+    state0 = z["state0"].copy().view(np.uint32).reshape(-1, 8)
+    starts = [certify.state_hash(state0)] + [str(e) for e in z["ends"][:-1]]
+    want = [f"segment {k} start {starts[k]} end {z['ends'][k]} flags {int(z['flags'][k])} "
+            f"status {int(z['status'][k])}" for k in range(len(z["ends"]))]
+    lines, _ = certify.segment_lines(gpu, z["image"].tobytes(), z["bank"].tobytes(), state0,
+                                     len(z["ends"]))
+    assert lines == want
