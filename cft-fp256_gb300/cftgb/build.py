@@ -18,6 +18,7 @@ ROOT = PKG.parent                                     # repository root
 CSRC = PKG / "csrc"
 OBJ = PKG / "_build"
 LIB = PKG / "lib" / "libcft_gb300.so"
+TOOL = PKG / "lib" / "cftg-asm"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
@@ -66,7 +67,22 @@ def build_lib(verbose=False):
         p = subprocess.run(cmd, capture_output=True, text=True)
         if p.returncode != 0:
             raise RuntimeError(f"link failed:\n{p.stdout}\n{p.stderr}")
+    build_tool()
     return LIB
+
+
+def build_tool():
+    """cftg-asm, the assembler command, over the library (host code only)."""
+    src = CSRC / "tools" / "cftg_asm.cpp"
+    if TOOL.exists() and TOOL.stat().st_mtime >= max(src.stat().st_mtime, LIB.stat().st_mtime):
+        return TOOL
+    cxx = os.environ.get("CXX") or shutil.which("g++") or "g++"
+    cmd = [cxx, "-O2", "-std=c++17", "-I", str(ROOT / "include"), str(src), "-o", str(TOOL),
+           "-L", str(LIB.parent), "-lcft_gb300", "-Wl,-rpath,$ORIGIN"]
+    p = subprocess.run(cmd, capture_output=True, text=True)
+    if p.returncode != 0:
+        raise RuntimeError(f"cftg-asm build failed:\n{p.stdout}\n{p.stderr}")
+    return TOOL
 
 
 def build_oracle():

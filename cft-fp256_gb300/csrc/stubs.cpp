@@ -64,15 +64,6 @@ extern "C" cft_status cft_formatof_mul(cft_device *, cft_format, cft_format, cft
 extern "C" cft_status cft_formatof_div(cft_device *, cft_format, cft_format, cft_round, const void *, const void *, void *, size_t, uint32_t *, uint32_t *) { clear_error(); return refuse("cft_formatof_div"); }
 extern "C" cft_status cft_formatof_sqrt(cft_device *, cft_format, cft_format, cft_round, const void *, void *, size_t, uint32_t *, uint32_t *) { clear_error(); return refuse("cft_formatof_sqrt"); }
 extern "C" cft_status cft_formatof_fma(cft_device *, cft_format, cft_format, cft_round, const void *, const void *, const void *, void *, size_t, uint32_t *, uint32_t *) { clear_error(); return refuse("cft_formatof_fma"); }
-// decimal digits a format needs to round-trip (754-2019 5.12.2: 1 + ceil(p log10 2)); a pure
-// function of the format, so it is answered rather than refused
-extern "C" size_t cft_format_decimal_digits(cft_format fmt)
-{
-    static const size_t d[4] = {9, 17, 36, 73};
-    return ((int)fmt >= 0 && (int)fmt <= 3) ? d[(int)fmt] : 0;
-}
-extern "C" cft_status cft_from_decimal_char(cft_device *, cft_format, cft_round, const char *const *, void *, size_t, size_t *, uint32_t *) { clear_error(); return refuse("cft_from_decimal_char"); }
-extern "C" cft_status cft_from_hex_char(cft_device *, cft_format, cft_round, const char *const *, void *, size_t, size_t *, uint32_t *) { clear_error(); return refuse("cft_from_hex_char"); }
 extern "C" cft_status cft_to_decimal_char(cft_device *, cft_format, cft_round, const void *, size_t, char *, size_t, size_t *, uint32_t *) { clear_error(); return refuse("cft_to_decimal_char"); }
 extern "C" cft_status cft_to_hex_char(cft_device *, cft_format, const void *, char *, size_t, size_t *) { clear_error(); return refuse("cft_to_hex_char"); }
 extern "C" cft_status cft_get_payload(cft_device *, cft_format, const void *, void *, size_t) { clear_error(); return refuse("cft_get_payload"); }

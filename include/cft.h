@@ -15,9 +15,11 @@
  *     GPU. There is no CPU fallback: without a GPU every open returns
  *     CFT_ERR_NO_DEVICE with a sentence saying so.
  *   - Operations outside the hot path (transcendentals, clause-5
- *     conversions, character I/O, formatOf, augmented arithmetic, the
- *     reductions) are exported so bindings load, and return
- *     CFT_ERR_UNSUPPORTED with a sentence naming the reason.
+ *     conversions, formatOf, the conversions to character sequences, NaN
+ *     payloads) are exported so bindings load, and return
+ *     CFT_ERR_UNSUPPORTED with a sentence naming the reason. The
+ *     reductions, the augmented operations and the conversions FROM
+ *     character sequences (which the program assembler needs) are built.
  */
 #ifndef CFT_H
 #define CFT_H
@@ -192,7 +194,8 @@ typedef struct cft_elem_args {
 CFT_API cft_status cft_run_ex(cft_device *dev, cft_op op, cft_format fmt, cft_round rnd,
                               const cft_elem_args *args);
 
-/* Reductions (cft.h:1210-1340): outside this backend's scope; refused. */
+/* Reductions (cft.h:1210-1340): SUM, DOT, SUMSQ, SUMABS and MAXALL over the
+ * reference's fixed tree, whole arrays and fixed-length segments. */
 CFT_API cft_status cft_reduce(cft_device *dev, cft_op op, cft_format fmt, cft_round rnd,
                               const void *a, const void *b, void *d, size_t n,
                               uint32_t *flags_out, uint32_t *bus_out);
@@ -212,6 +215,20 @@ CFT_API cft_status cft_augmented_sub(cft_device *dev, cft_format fmt, const void
                                      uint32_t *flags_out);
 CFT_API cft_status cft_augmented_mul(cft_device *dev, cft_format fmt, const void *a,
                                      const void *b, void *r, void *e, size_t n,
+                                     uint32_t *flags_out);
+
+/* ---- character sequences to encodings, 754-2019 5.12 (cft.h:1899-1960) *
+ * Host operations: a batch of NUL-terminated sequences, each correctly
+ * rounded under rnd into fmt with exact flags (OR across the batch); NaN
+ * payloads and the signalling bit kept. A sequence outside the syntax
+ * refuses the whole call with CFT_ERR_INVALID_ARGUMENT and its index in
+ * *bad_index. cft_format_decimal_digits is 5.12.2's Pmin: 9, 17, 36, 73. */
+CFT_API size_t cft_format_decimal_digits(cft_format fmt);
+CFT_API cft_status cft_from_decimal_char(cft_device *dev, cft_format fmt, cft_round rnd,
+                                         const char *const *in, void *d, size_t n,
+                                         size_t *bad_index, uint32_t *flags_out);
+CFT_API cft_status cft_from_hex_char(cft_device *dev, cft_format fmt, cft_round rnd,
+                                     const char *const *in, void *d, size_t n, size_t *bad_index,
                                      uint32_t *flags_out);
 
 /* ---- resident buffers (cft.h:2470-2705) ------------------------------- *

@@ -285,6 +285,38 @@ CFT_API void cftg_server_get_stats(cftg_server *s, cftg_server_stats *out);
 /* Finishes every queued request, stops the engine and frees the budget. */
 CFT_API void cftg_server_free(cftg_server *s);
 
+/* ---- programs as source: the `.cfta` assembler (host only) ------------
+ *
+ * The reference's text form (docs/PROGRAMS.md; python/cft_golden/asm.py,
+ * host/tools/cft-asm.c) as library calls, so a client can submit SOURCE.
+ * cftg_asm_assemble turns UTF-8 text into the exact `.cftp` image the
+ * reference assembler writes (*image malloc'd, freed with cftg_asm_free),
+ * or refuses with CFT_ERR_INVALID_ARGUMENT and "source:line: reason" in
+ * cft_last_error(). cftg_asm_disassemble gives text that assembles back to
+ * the same bytes; cftg_asm_info the header report of `cft-asm -i`. None
+ * needs a device. cftg_program_load_source assembles and loads in one call.
+ *
+ * cftg_ode_bank writes the default bank of one of the reference's ODE
+ * segment programs ("lorenz63-rk4", "lorenz96-rk4", "henonheiles-lf") for a
+ * step h given as a decimal, as programs/gen_odes.py:bank_values derives
+ * it: raw format-width values, dense, in declaration order. *bytes is set
+ * to the size needed; bank NULL with cap 0 asks for it. */
+CFT_API cft_status cftg_asm_assemble(const char *text, size_t len, const char *source,
+                                     void **image, size_t *image_bytes);
+CFT_API cft_status cftg_asm_disassemble(const void *image, size_t bytes, char **text);
+CFT_API cft_status cftg_asm_info(const void *image, size_t bytes, char **text);
+CFT_API void cftg_asm_free(void *p);
+CFT_API cft_status cftg_ode_bank(const char *system, cft_format fmt, const char *h, void *bank,
+                                 size_t cap, size_t *bytes);
+CFT_API cft_status cftg_program_load_source(cft_device *dev, const char *text, size_t len,
+                                            const char *source, cft_program **out);
+
+/* One decimal (hex = 0) or hexadecimal-significand (hex = 1) sequence into
+ * fmt under rnd, exactly as cft_from_decimal_char / cft_from_hex_char
+ * convert each element, with no device: the form tools use. */
+CFT_API cft_status cftg_from_char(int hex, cft_format fmt, cft_round rnd, const char *in, void *d,
+                                  uint32_t *flags_out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -70,10 +70,7 @@ CFT_API cft_status cft_formatof_mul(cft_device *dev, cft_format sfmt, cft_format
 CFT_API cft_status cft_formatof_div(cft_device *dev, cft_format sfmt, cft_format dfmt, cft_round rnd, const void *a, const void *b, void *d, size_t n, uint32_t *flags_out, uint32_t *bus_out);
 CFT_API cft_status cft_formatof_sqrt(cft_device *dev, cft_format sfmt, cft_format dfmt, cft_round rnd, const void *a, void *d, size_t n, uint32_t *flags_out, uint32_t *bus_out);
 CFT_API cft_status cft_formatof_fma(cft_device *dev, cft_format sfmt, cft_format dfmt, cft_round rnd, const void *a, const void *b, const void *c, void *d, size_t n, uint32_t *flags_out, uint32_t *bus_out);
-/* character conversions and payloads, 754-2019 5.12 and 9.7 (cft.h:1899-2002) */
-CFT_API size_t cft_format_decimal_digits(cft_format fmt);
-CFT_API cft_status cft_from_decimal_char(cft_device *dev, cft_format fmt, cft_round rnd, const char *const *in, void *d, size_t n, size_t *bad_index, uint32_t *flags_out);
-CFT_API cft_status cft_from_hex_char(cft_device *dev, cft_format fmt, cft_round rnd, const char *const *in, void *d, size_t n, size_t *bad_index, uint32_t *flags_out);
+/* conversions to character sequences and payloads, 754-2019 5.12 and 9.7 (cft.h:1936-2002) */
 CFT_API cft_status cft_to_decimal_char(cft_device *dev, cft_format fmt, cft_round rnd, const void *a, size_t digits, char *out, size_t cap, size_t *len, uint32_t *flags_out);
 CFT_API cft_status cft_to_hex_char(cft_device *dev, cft_format fmt, const void *a, char *out, size_t cap, size_t *len);
 CFT_API cft_status cft_get_payload(cft_device *dev, cft_format fmt, const void *a, void *d, size_t n);
