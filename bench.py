@@ -384,6 +384,8 @@ def main():
                     help="serving suite: element batches on the device at once")
     ap.add_argument("--program-inflight", type=int, default=2,
                     help="serving suite: program batches on the device at once")
+    ap.add_argument("--elem-blocks-per-sm", type=int, default=0,
+                    help="serving suite: work-queue blocks an SM per element batch (0: the server's default, two)")
     ap.add_argument("--seconds", type=float, default=60.0,
                     help="length of the serving suite's request stream")
     ap.add_argument("--fmt", type=int, default=3, help="format of the headline leg (3 = binary256)")
@@ -411,7 +413,8 @@ def main():
             print(json.dumps(suites.serving(h, z["hh_image"], z["hh_bank"], rate=args.rate,
                                             seconds=args.seconds, program_frac=args.program_frac,
                                             max_inflight=args.inflight,
-                                            max_program_inflight=args.program_inflight)))
+                                            max_program_inflight=args.program_inflight,
+                                            elem_blocks_per_sm=args.elem_blocks_per_sm)))
         else:
             print(json.dumps(getattr(suites, args.suite)(h)))
         cftgb.close_device(h)

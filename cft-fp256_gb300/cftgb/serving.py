@@ -13,7 +13,7 @@ class ServerConfig(ctypes.Structure):
     _fields_ = [("struct_size", ctypes.c_size_t), ("hbm_budget", ctypes.c_uint64),
                 ("max_inflight", ctypes.c_uint32), ("max_program_inflight", ctypes.c_uint32),
                 ("max_batch_calls", ctypes.c_uint32), ("max_batch_lanes", ctypes.c_uint32),
-                ("max_batch_elements", ctypes.c_uint64)]
+                ("max_batch_elements", ctypes.c_uint64), ("elem_blocks_per_sm", ctypes.c_uint32)]
 
 
 class Request(ctypes.Structure):
@@ -75,11 +75,11 @@ class Server:
     it after every queued request has finished."""
 
     def __init__(self, h, budget, max_inflight=4, max_program_inflight=4, max_batch_calls=4096,
-                 max_batch_lanes=65536, max_batch_elements=0):
+                 max_batch_lanes=65536, max_batch_elements=0, elem_blocks_per_sm=0):
         self.L = _lib.lib()
         _bind(self.L)
         cfg = ServerConfig(ctypes.sizeof(ServerConfig), budget, max_inflight, max_program_inflight,
-                           max_batch_calls, max_batch_lanes, max_batch_elements)
+                           max_batch_calls, max_batch_lanes, max_batch_elements, elem_blocks_per_sm)
         self.s = vp()
         _lib.check(self.L.cftg_server_create(h, ctypes.byref(cfg), ctypes.byref(self.s)),
                    "cftg_server_create")

@@ -369,7 +369,7 @@ def hh_init(lanes, seed):
 
 def serving(h, hh_image, hh_bank, rate=20000.0, seconds=60.0, seed=5, budget=40 << 30,
             program_frac=0.02, hh_lanes=32, max_log2=22, sample_every=2000, max_inflight=6,
-            max_program_inflight=2, max_batch_elements=1 << 24):
+            max_program_inflight=2, max_batch_elements=1 << 24, elem_blocks_per_sm=0):
     """Open-loop serving: requests arrive as a Poisson stream of `rate` a
     second for `seconds`; each is an element call (binary128 or binary256
     1:1, size log-uniform in [64, 2^max_log2], operation uniform over add,
@@ -426,7 +426,8 @@ def serving(h, hh_image, hh_bank, rate=20000.0, seconds=60.0, seed=5, budget=40 
     comp = []
     with sv.Server(h, budget, max_inflight=max_inflight, max_program_inflight=max_program_inflight,
                    max_batch_calls=4096, max_batch_lanes=1 << 16,
-                   max_batch_elements=max_batch_elements) as srv:
+                   max_batch_elements=max_batch_elements,
+                   elem_blocks_per_sm=elem_blocks_per_sm) as srv:
         t0 = sv.clock_ns() + 20_000_000
         arr_ns = (t0 + arrive * 1e9).astype(np.int64)
         i = loops = 0

@@ -475,7 +475,8 @@ extern "C" cft_status cftg_server_create(cft_device *dev, const cftg_server_conf
                                          cftg_server **out)
 {
     clear_error();
-    if (!dev || !cfg || !out || cfg->struct_size < sizeof(cftg_server_config)) {
+    // a config written before elem_blocks_per_sm existed is read with it 0
+    if (!dev || !cfg || !out || cfg->struct_size < offsetof(cftg_server_config, elem_blocks_per_sm)) {
         set_error("cftg_server_create: needs a device, a config (struct_size set) and out");
         return CFT_ERR_INVALID_ARGUMENT;
     }
@@ -484,7 +485,8 @@ extern "C" cft_status cftg_server_create(cft_device *dev, const cftg_server_conf
         set_error("cftg_server_create: the handle is poisoned by an earlier device failure");
         return CFT_ERR_INTERNAL;
     }
-    cftg_server_config c = *cfg;
+    cftg_server_config c{};
+    memcpy(&c, cfg, std::min(cfg->struct_size, sizeof c));
     if (!c.hbm_budget || c.max_inflight < 1 || c.max_inflight > 16 || c.max_program_inflight > 16 ||
         c.max_batch_calls < 1 || c.max_batch_calls > (1u << 20) ||
         (c.max_program_inflight && (c.max_batch_lanes < 1 || c.max_batch_lanes > (1u << 24)))) {
@@ -496,7 +498,11 @@ extern "C" cft_status cftg_server_create(cft_device *dev, const cftg_server_conf
     if (!s) return CFT_ERR_OUT_OF_MEMORY;
     s->dev = dev;
     s->cfg = c;
-    s->queue_blocks = sm_count() * queue_blocks_per_sm();
+    {
+        const int per = queue_blocks_per_sm();
+        const int want = (int)std::min<uint32_t>(c.elem_blocks_per_sm ? c.elem_blocks_per_sm : 2u, (uint32_t)per);
+        s->queue_blocks = sm_count() * want;
+    }
     cudaSetDevice(dev->ordinal);
     bool ok = cudaMalloc(&s->base, c.hbm_budget) == cudaSuccess;
     s->arena.init(c.hbm_budget);

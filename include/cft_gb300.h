@@ -232,6 +232,12 @@ typedef struct {
     uint64_t max_batch_elements;    /* elements of one element batch (0: no limit); a batch
                                        completes as a whole, so this bounds the wait of its
                                        smallest requests */
+    uint32_t elem_blocks_per_sm;    /* work-queue blocks an SM per element batch (0: two;
+                                       clamped to what fits an empty SM). A batch completes when
+                                       its last block has run, so a block that does not fit
+                                       beside the trajectory blocks already on an SM waits for
+                                       them to finish: two leave room for them and keep every
+                                       element block resident */
 } cftg_server_config;
 
 #define CFTG_REQ_ELEM    0
