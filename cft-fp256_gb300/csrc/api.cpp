@@ -674,6 +674,17 @@ static bool exec_direct(const char *who, cft_device *dev, int kind, int op, int 
     L.n = n;
     L.scalar_mask = scalar_mask & 7u;
     L.flags = dev->d_word;
+    // Two blocks an SM: the host link carries ~211 GB/s, which a few warps an
+    // SM saturate, and more requests in flight over it lower what it carries
+    // (fp256 FMA in place: 2.13 Gelem/s at one or two blocks an SM, 1.83 at
+    // three, 1.65 at four). CFTG_HOST_BLOCKS_PER_SM overrides.
+    {
+        static const int per = [] {
+            const char *v = getenv("CFTG_HOST_BLOCKS_PER_SM");
+            return v && atoi(v) > 0 ? atoi(v) : 2;
+        }();
+        L.blocks_per_sm = (uint32_t)per;
+    }
     cudaError_t e = cudaMemsetAsync(dev->d_word, 0, sizeof(uint32_t), s);
     if (e == cudaSuccess) e = launch_elem(L, s);
     if (e == cudaSuccess)

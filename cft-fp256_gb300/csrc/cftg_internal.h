@@ -31,6 +31,7 @@ struct ElemLaunch {
     size_t n = 0;
     uint32_t *flags = nullptr;                // device word, ORed into
     uint8_t *lane_flags = nullptr;            // optional, n bytes
+    uint32_t blocks_per_sm = 0;               // grid cap in blocks an SM (0: eight)
 };
 
 // Launch on `stream`; returns the launch status.

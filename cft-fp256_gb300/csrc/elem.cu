@@ -111,7 +111,7 @@ static cudaError_t go(const ElemLaunch &L, cudaStream_t s)
 {
     constexpr int T = 256;
     const size_t want = (L.n + T - 1) / T;
-    const size_t cap = (size_t)sm_count() * 8;
+    const size_t cap = (size_t)sm_count() * (L.blocks_per_sm ? L.blocks_per_sm : 8u);
     const unsigned blocks = (unsigned)(want < cap ? want : cap);
     k_elem<FMT, KIND><<<blocks ? blocks : 1, T, 0, s>>>(L);
     return cudaGetLastError();

@@ -67,27 +67,30 @@ SFD void shl(uint32_t (&x)[N], int s)
 
 // x >>= s with every bit shifted out ORed into bit 0 ("jamming").
 // Any s: s <= 0 leaves x alone, s >= 32N leaves only the jam. Branch-free.
+// The jam is gathered as the words leave: each stage of the select network
+// that shifts drops its low b words, and the funnel shift drops the low bs
+// bits of what is then x[0].
 template <int N>
 SFD void shr_jam(uint32_t (&x)[N], int s)
 {
     const int sc = s <= 0 ? 0 : (s >= 32 * N ? 32 * N : s);
     const int ws = sc >> 5, bs = sc & 31;                 // ws may be N
     uint32_t st = 0u;
-#pragma unroll
-    for (int i = 0; i < N; i++) {
-        const uint32_t m = (i < ws) ? 0xFFFFFFFFu : (i == ws ? ((1u << bs) - 1u) : 0u);
-        st |= x[i] & m;
-    }
     const int need = warp_stages(ws);
 #pragma unroll
     for (int b = 16; b >= 1; b >>= 1) {
         if (b <= N && (need & b)) {
             const bool take = (ws & b) != 0;
+            uint32_t out = 0u;
+#pragma unroll
+            for (int i = 0; i < b; i++) out |= x[i];
+            st |= take ? out : 0u;
 #pragma unroll
             for (int i = 0; i < N; i++)
                 x[i] = take ? (i + b < N ? x[i + b] : 0u) : x[i];
         }
     }
+    st |= x[0] & ((1u << bs) - 1u);
 #pragma unroll
     for (int i = 0; i < N - 1; i++) x[i] = __funnelshift_r(x[i], x[i + 1], bs);
     x[N - 1] >>= bs;
@@ -112,6 +115,19 @@ SFD void shr(uint32_t (&x)[N], int s)
 #pragma unroll
     for (int i = 0; i < N - 1; i++) x[i] = __funnelshift_r(x[i], x[i + 1], bs);
     x[N - 1] >>= bs;
+}
+
+// x <<= S for a compile-time 0 <= S < 32N, zero fill.
+template <int S, int N>
+SFD void shl_const(uint32_t (&x)[N])
+{
+    constexpr int ws = S >> 5, bs = S & 31;
+#pragma unroll
+    for (int i = N - 1; i >= 0; i--) {
+        const uint32_t hi = (i - ws >= 0) ? x[i - ws] : 0u;
+        const uint32_t lo = (i - ws - 1 >= 0) ? x[i - ws - 1] : 0u;
+        x[i] = bs ? __funnelshift_l(lo, hi, bs) : hi;
+    }
 }
 
 // x >>= s for a compile-time 0 <= S < 32N (no jam).

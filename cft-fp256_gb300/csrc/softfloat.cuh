@@ -69,8 +69,10 @@ SFD int sign_of(const uint32_t (&x)[Fmt<FMT>::W])
     return (int)(x[Fmt<FMT>::W - 1] >> 31);
 }
 
-// Classify and unpack (host/src/softfloat.c:85-116 gives the classes).
-template <int FMT>
+// Classify and unpack (host/src/softfloat.c:85-116 gives the classes). A
+// finite non-zero significand is normalised with its leading bit at bit LB
+// of the W words (32W-1 unless a caller wants it lower).
+template <int FMT, int LB = 32 * Fmt<FMT>::W - 1>
 SFD void unpack(const uint32_t (&x)[Fmt<FMT>::W], Unp<FMT> &u)
 {
     using F = Fmt<FMT>;
@@ -93,13 +95,13 @@ SFD void unpack(const uint32_t (&x)[Fmt<FMT>::W], Unp<FMT> &u)
         u.cls = C_SUB;
         const int L = sfw::bitlen(u.m);
         u.ve = F::EMIN - F::MANW + L - 1;
-        sfw::shl(u.m, 32 * W - L);
+        sfw::shl(u.m, LB + 1 - L);
         return;
     }
     u.cls = C_NORM;
     u.m[W - 1] |= 1u << exp_shift<FMT>();                  // hidden bit
     u.ve = (int)ef - F::BIAS;
-    sfw::shl(u.m, 32 * W - F::P);
+    sfw::shl_const<LB - F::MANW>(u.m);
 }
 
 // ---- encodings ---------------------------------------------------------
@@ -186,7 +188,9 @@ SFD void take_top(const uint32_t (&m)[N], uint32_t (&kept)[Fmt<FMT>::W], bool &g
 // Round the exact non-zero value m * 2^e (m an N-word integer; its bit 0 may
 // carry a jammed sticky, which must sit at least two places below the
 // rounding point) into the format. Writes the encoding and the flags.
-template <int FMT, int N>
+// ZERO: m may be zero (an exact cancellation), which gives +0, or -0 under
+// roundTowardNegative, with no flag.
+template <int FMT, int N, bool ZERO = false>
 SFD void round_pack(int sign, uint32_t (&m)[N], int e, int rnd, uint32_t (&out)[Fmt<FMT>::W],
                     uint32_t &flags)
 {
@@ -199,7 +203,16 @@ SFD void round_pack(int sign, uint32_t (&m)[N], int e, int rnd, uint32_t (&out)[
     int L;
     if (__all_sync(am, m[N - 1] != 0u)) L = 32 * N - __clz(m[N - 1]);
     else if (__all_sync(am, m[N - 1] == 0u && m[N - 2] != 0u)) L = 32 * (N - 1) - __clz(m[N - 2]);
-    else L = sfw::bitlen(m);
+    else {
+        L = sfw::bitlen(m);
+        if constexpr (ZERO) {
+            if (L == 0) {
+                enc_zero<FMT>(out, rnd == RDN ? 1 : 0);
+                flags = 0u;
+                return;
+            }
+        }
+    }
     const int e_norm = e + L - 1;                 // exponent of the leading bit
     sfw::shl(m, 32 * N - L);                      // leading bit to the top
 
@@ -208,15 +221,15 @@ SFD void round_pack(int sign, uint32_t (&m)[N], int e, int rnd, uint32_t (&out)[
     take_top<FMT, N>(m, kept, guard, sticky);
     bool up = round_up(rnd, sign, guard, sticky, kept[0] & 1u);
 
-    // Rounded as if the exponent range were unbounded: does it carry out?
-    uint32_t ones[W];
-#pragma unroll
-    for (int i = 0; i < W; i++) ones[i] = 0xFFFFFFFFu;
-    ones[W - 1] = (F::P % 32) ? ((1u << (F::P % 32)) - 1u) : 0xFFFFFFFFu;
-    const bool carry_unb = up && sfw::cmp(kept, ones) == 0;
-
     const int d = F::EMIN - e_norm;              // > 0: below the normal range
+    bool carry_unb = false;
     if (d > 0) {
+        // Rounded as if the exponent range were unbounded: does it carry out?
+        uint32_t ones[W];
+#pragma unroll
+        for (int i = 0; i < W; i++) ones[i] = 0xFFFFFFFFu;
+        ones[W - 1] = (F::P % 32) ? ((1u << (F::P % 32)) - 1u) : 0xFFFFFFFFu;
+        carry_unb = up && sfw::cmp(kept, ones) == 0;
         sfw::shr_jam(m, d);
         take_top<FMT, N>(m, kept, guard, sticky);
         up = round_up(rnd, sign, guard, sticky, kept[0] & 1u);
@@ -272,10 +285,11 @@ enum { OP_FMA = 0, OP_ADD = 1, OP_SUB = 2, OP_MUL = 3 };
 
 // The general path: finite non-zero a and b; c finite (zero allowed).
 //
-// Window: N = 2W words. a's significand is placed with its leading bit at
-// 32W-2 and b's at 32W-1, so their product's leading bit is at 64W-3 or
-// 64W-2 and bit 64W-1 is free for a carry. Its low 64W-2P-1 bits are zero.
-// The addend's leading bit is aligned to 64W-2, its low 64W-P-1 bits zero.
+// Window: N = 2W words. a's significand arrives with its leading bit at
+// 32W-2 and b's at 32W-1 (unpack<FMT, LB>), so their product's leading bit
+// is at 64W-3 or 64W-2 and bit 64W-1 is free for a carry. Its low 64W-2P-1
+// bits are zero. The addend (leading bit at 32W-2) goes to the top half, its
+// leading bit at 64W-2, its low 64W-P-1 bits zero.
 // With delta = (addend exponent) - (product's nominal exponent) - 1:
 //  * delta > 0: the product is shifted right by delta. Exact for delta <= 1
 //    (the only shifts after which the two can cancel to fewer than P+2
@@ -304,15 +318,11 @@ SFD void fma_general(const Unp<FMT> &ua, const Unp<FMT> &ub, const Unp<FMT> &uc,
 #pragma unroll
         for (int i = 0; i < W; i++) P[i] = 0u;
 #pragma unroll
-        for (int i = 0; i < W; i++) P[W + i] = ua.m[i];   // leading bit at 64W-1
-        sfw::shr_const<2>(P);                              // leading bit at 64W-3
+        for (int i = 0; i < W; i++) P[W + i] = ua.m[i];   // leading bit at 64W-2
+        sfw::shr_const<1>(P);                              // leading bit at 64W-3
         ew = ua.ve - (64 * W - 3);
     } else {
-        uint32_t ma[W];
-#pragma unroll
-        for (int i = 0; i < W; i++) ma[i] = ua.m[i];
-        sfw::shr_const<1>(ma);                     // leading bit at 32W-2
-        sfw::mul_ptx<W>(P, ma, ub.m);
+        sfw::mul_ptx<W>(P, ua.m, ub.m);
         ew = ua.ve + ub.ve - (64 * W - 3);
     }
 
@@ -324,7 +334,6 @@ SFD void fma_general(const Unp<FMT> &ua, const Unp<FMT> &ub, const Unp<FMT> &uc,
         for (int i = 0; i < W; i++) C[i] = 0u;
 #pragma unroll
         for (int i = 0; i < W; i++) C[W + i] = uc.m[i];
-        sfw::shr_const<1>(C);
         const bool czero = uc.cls == C_ZERO;
         if (czero) {
 #pragma unroll
@@ -368,13 +377,10 @@ SFD void fma_general(const Unp<FMT> &ua, const Unp<FMT> &ub, const Unp<FMT> &uc,
             }
         }
         rs = neg ? s_small : s_big;
-        if (sub && sfw::is_zero(P)) {              // exact cancellation
-            enc_zero<FMT>(out, rnd == RDN ? 1 : 0);
-            flags = 0u;
-            return;
-        }
     }
-    round_pack<FMT, N>(rs, P, ew, rnd, out, flags);
+    // an exact cancellation (only an effective subtraction gives one) leaves
+    // P zero, which round_pack answers with the zero of the attribute
+    round_pack<FMT, N, OP != OP_MUL>(rs, P, ew, rnd, out, flags);
 }
 
 // One element of FMA/ADD/SUB/MUL. x/y/z are the caller's a, b, c (b unused
@@ -403,9 +409,9 @@ SFD void arith(const uint32_t (&x)[Fmt<FMT>::W], const uint32_t (&y)[Fmt<FMT>::W
         for (int i = 0; i < W; i++) csteer[i] = z[i];
         if constexpr (OP == OP_SUB) csteer[W - 1] ^= 0x80000000u;
     }
-    unpack<FMT>(x, ua);
-    unpack<FMT>(bsteer, ub);
-    unpack<FMT>(csteer, uc);
+    unpack<FMT, 32 * W - 2>(x, ua);
+    unpack<FMT, 32 * W - 1>(bsteer, ub);
+    unpack<FMT, 32 * W - 2>(csteer, uc);
     flags = 0u;
 
     if (ua.cls == C_NAN || ub.cls == C_NAN || uc.cls == C_NAN) {
