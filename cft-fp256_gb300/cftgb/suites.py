@@ -1,6 +1,6 @@
 """Benchmark suites beside the headline (bench.py --suite NAME): each
-measures one of the configurations the project is judged on and returns
-a dict that bench.py prints as one JSON line.
+measures one of the path's benchmark configurations and returns a dict
+that bench.py prints as one JSON line.
 
 uneven  10,000 independent elementwise calls, sizes log-uniform in
         [1, 2^20], formats fp64/fp128/fp256 drawn 0.2/0.4/0.4, operation
