@@ -369,7 +369,8 @@ def hh_init(lanes, seed):
 
 def serving(h, hh_image, hh_bank, rate=20000.0, seconds=60.0, seed=5, budget=40 << 30,
             program_frac=0.02, hh_lanes=32, max_log2=22, sample_every=2000, max_inflight=6,
-            max_program_inflight=2, max_batch_elements=1 << 24, elem_blocks_per_sm=0):
+            max_program_inflight=2, max_batch_elements=1 << 24, elem_blocks_per_sm=0,
+            sample_max_n=1 << 20):
     """Open-loop serving: requests arrive as a Poisson stream of `rate` a
     second for `seconds`; each is an element call (binary128 or binary256
     1:1, size log-uniform in [64, 2^max_log2], operation uniform over add,
@@ -378,8 +379,11 @@ def serving(h, hh_image, hh_bank, rate=20000.0, seconds=60.0, seed=5, budget=40 
     ensemble of hh_lanes lanes at binary256 (h = 1e-3, energy 1/8) for
     1e3..1e4 steps (log-uniform). The server admits them by a budget of
     `budget` bytes. Latency is completion time minus scheduled arrival.
-    Every sample_every-th request keeps its output for the comparison with
-    the same request run alone."""
+    Every sample_every-th request (element requests of at most
+    sample_max_n elements) keeps its output, in pinned memory allocated
+    before the stream starts, for the comparison with the same request run
+    alone: pinning memory while requests arrive would stall the submitting
+    thread and charge the stall to the requests behind it."""
     import torch
     from . import serving as sv
     from . import workload as wl
@@ -421,6 +425,20 @@ def serving(h, hh_image, hh_bank, rate=20000.0, seconds=60.0, seed=5, budget=40 
     which_init = rng.integers(0, 16, size=count)
     OPS = SWEEP_OPS
     base = {f: [x.data_ptr() for x in pools[f]] for f in (2, 3)}
+    # the sampled requests and their output buffers, carved from one pinned
+    # block allocated now
+    sampled, nxt = set(), 0
+    for i in range(count):
+        if i >= nxt and (is_prog[i] or sizes[i] <= sample_max_n):
+            sampled.add(i)
+            nxt = (i // sample_every + 1) * sample_every
+    out_bytes = {i: (inits[0].nbytes if is_prog[i] else int(sizes[i]) * 4 * wl.words(int(fmts[i])))
+                 for i in sampled}
+    pinned = torch.empty(max(1, sum(out_bytes.values())), dtype=torch.uint8, pin_memory=True)
+    out_views, off = {}, 0
+    for i in sorted(sampled):
+        out_views[i] = pinned[off:off + out_bytes[i]]
+        off += out_bytes[i]
     samples = {}
     req = sv.Request()
     comp = []
@@ -434,7 +452,7 @@ def serving(h, hh_image, hh_bank, rate=20000.0, seconds=60.0, seed=5, budget=40 
         while i < count:
             now = sv.clock_ns()
             while i < count and arr_ns[i] <= now:
-                sample = (i % sample_every) == 0
+                sample = i in sampled
                 req.tag = i
                 req.t_arrival_ns = int(arr_ns[i])
                 req.host_out = None
@@ -448,7 +466,7 @@ def serving(h, hh_image, hh_bank, rate=20000.0, seconds=60.0, seed=5, budget=40 
                     req.runs = int(runs[i])
                     req.n = 0
                     if sample:
-                        out = torch.empty(init.nbytes, dtype=torch.uint8, pin_memory=True)
+                        out = out_views[i]
                         req.host_out = out.data_ptr()
                         samples[i] = ("prog", int(which_init[i]), int(runs[i]), out)
                 else:
@@ -463,7 +481,7 @@ def serving(h, hh_image, hh_bank, rate=20000.0, seconds=60.0, seed=5, budget=40 
                     req.n = n
                     req.prog = None
                     if sample:
-                        out = torch.empty(n * esz, dtype=torch.uint8, pin_memory=True)
+                        out = out_views[i]
                         req.host_out = out.data_ptr()
                         samples[i] = ("elem", kind, op, f, int(rnds[i]), req.d_a, req.d_b, req.d_c,
                                       n, out)

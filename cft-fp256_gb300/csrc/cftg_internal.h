@@ -130,6 +130,11 @@ struct TrajLaunch {
     const uint64_t *b_ops = nullptr;
     const uint32_t *b_ctl = nullptr, *b_arg = nullptr;
     const int32_t *b_match = nullptr;
+    // A caller sharing the GPU with other kernels caps how many of this
+    // launch's blocks an SM holds: at most as many as fit in sm_regs
+    // registers, enforced by asking each block for a share of sm_smem bytes
+    // of shared memory. 0: no cap.
+    uint32_t sm_regs = 0, sm_smem = 0;
 };
 
 cudaError_t launch_traj(const TrajLaunch &L, cudaStream_t stream);

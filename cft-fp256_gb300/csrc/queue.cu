@@ -198,6 +198,16 @@ cudaError_t launch_queue(const QCall *calls, const QTile *tiles, uint32_t ntiles
     return cudaGetLastError();
 }
 
+int queue_calls_regs()
+{
+    cudaFuncAttributes fa;
+    if (cudaFuncGetAttributes(&fa, k_queue_calls) != cudaSuccess) {
+        cudaGetLastError();
+        return 255;
+    }
+    return fa.numRegs;
+}
+
 int queue_blocks_per_sm()
 {
     int per = 0;

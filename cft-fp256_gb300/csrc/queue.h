@@ -25,6 +25,8 @@ struct QTile {
 cudaError_t launch_queue(const QCall *calls, const QTile *tiles, uint32_t ntiles, uint32_t *counter,
                          uint32_t *call_flags, int blocks, cudaStream_t s);
 int queue_blocks_per_sm();
+// Registers a thread of the table-free work-queue kernel uses.
+int queue_calls_regs();
 
 // The same work queue without a tile table: call i owns tiles
 // [prefix[i], prefix[i+1]) of `tile` elements each (the last one short), so

@@ -701,6 +701,29 @@ static cudaError_t smem_ceiling_once(K kernel, unsigned &done_mask)
     return e;
 }
 
+// The shared memory a trajectory block asks for so that an SM holds no more
+// of this launch's blocks than L.sm_regs registers allow (TrajLaunch).
+template <typename K>
+static size_t capped_smem(K kernel, const TrajLaunch &L, int threads, size_t smem)
+{
+    if (!L.sm_regs || !L.sm_smem) return smem;
+    cudaFuncAttributes fa;
+    if (cudaFuncGetAttributes(&fa, kernel) != cudaSuccess) {
+        cudaGetLastError();
+        return smem;
+    }
+    int dev = 0, reserved = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev);
+    // registers are allocated a warp at a time, in units of 256
+    const size_t warp_regs = ((size_t)fa.numRegs * 32 + 255) / 256 * 256;
+    const size_t block_regs = warp_regs * (size_t)((threads + 31) / 32);
+    size_t k = L.sm_regs / block_regs;
+    if (k < 1) k = 1;
+    const long each = (long)(L.sm_smem / k) - reserved - (long)fa.sharedSizeBytes;
+    return each > (long)smem ? (size_t)each / 1024 * 1024 : smem;
+}
+
 template <int FMT>
 static int seq_threads(const SeqProgram &P, size_t *smem)
 {
@@ -734,6 +757,7 @@ static cudaError_t go_traj(const TrajLaunch &L, cudaStream_t s)
     const size_t scr = (size_t)L.P.reach * W * 4;
     const bool shared = L.P.reach > 0 && (regs + scr) * T <= (160u << 10);
     if (shared) smem += scr * T;
+    smem = capped_smem(k_traj<FMT>, L, T, smem);
     static unsigned done = 0;
     cudaError_t e = smem_ceiling_once(k_traj<FMT>, done);
     if (e != cudaSuccess) return e;
@@ -747,7 +771,7 @@ static cudaError_t go_traj_g(const TrajLaunch &L, cudaStream_t s)
 {
     constexpr int W = sf::Fmt<FMT>::W;
     const int LPB = 32 / L.G;
-    const size_t smem = (size_t)L.nloc * (size_t)(W * LPB + 1) * 4;
+    const size_t smem = capped_smem(k_traj_g<FMT>, L, 32, (size_t)L.nloc * (size_t)(W * LPB + 1) * 4);
     static unsigned done = 0;
     cudaError_t e = smem_ceiling_once(k_traj_g<FMT>, done);
     if (e != cudaSuccess) return e;

@@ -90,6 +90,12 @@ struct cftg_server {
     // three program streams stay within the queues.
     std::vector<cudaStream_t> streams;
     int queue_blocks = 0;
+    // The registers and shared memory of an SM that trajectory blocks may
+    // take: what the element batches' blocks leave. Each trajectory launch
+    // asks its blocks for shared memory so that no more of them fit than
+    // these registers hold, so element blocks always find room beside them,
+    // however many program batches are in flight.
+    uint32_t traj_sm_regs = 0, traj_sm_smem = 0;
 
     std::mutex mu;                  // intake, completions, counters below
     std::condition_variable cv_in, cv_done;
@@ -293,6 +299,8 @@ bool cftg_server::launch_prog(Slot &sl)
     T.lane_status = sl.d_lstatus;
     T.word = sl.d_word;
     plan_lanes(head->r.prog, lanes, T);
+    T.sm_regs = traj_sm_regs;
+    T.sm_smem = traj_sm_smem;
     if (e == cudaSuccess) e = launch_traj(T, sl.s);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(sl.h_lflags, sl.d_lflags, lanes, cudaMemcpyDeviceToHost, sl.s);
@@ -502,6 +510,15 @@ extern "C" cft_status cftg_server_create(cft_device *dev, const cftg_server_conf
         const int per = queue_blocks_per_sm();
         const int want = (int)std::min<uint32_t>(c.elem_blocks_per_sm ? c.elem_blocks_per_sm : 2u, (uint32_t)per);
         s->queue_blocks = sm_count() * want;
+        int per_sm = 0, reserved = 0, regs_sm = 0;
+        cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev->ordinal);
+        cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev->ordinal);
+        cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev->ordinal);
+        const long elem_regs = (long)want * 256 * ((queue_calls_regs() * 32 + 255) / 256 * 256) / 32;
+        const long regs_left = (long)regs_sm - elem_regs;
+        const long smem_left = (long)per_sm - (long)want * (reserved + 1024);
+        s->traj_sm_regs = regs_left > 0 ? (uint32_t)regs_left : 1u;
+        s->traj_sm_smem = smem_left > 0 ? (uint32_t)smem_left : 0u;
     }
     cudaSetDevice(dev->ordinal);
     bool ok = cudaMalloc(&s->base, c.hbm_budget) == cudaSuccess;
