@@ -135,6 +135,18 @@ struct TrajLaunch {
     // registers, enforced by asking each block for a share of sm_smem bytes
     // of shared memory. 0: no cap.
     uint32_t sm_regs = 0, sm_smem = 0;
+    // Completion a request at a time (the serving loop), when req_of is
+    // set: lane l belongs to request req_of[l], whose lanes start at batch
+    // lane req_lane0[r]. A lane that has run its last segment writes its
+    // final block to state and, when req_out[r] is not NULL (host memory the
+    // GPU writes), to req_out[r] at its place in the request; ORs its flags
+    // and STATUS into req_acc[2r], req_acc[2r+1] and counts req_left[r]
+    // down. The request's last lane writes the flags and STATUS to
+    // req_done[4r], req_done[4r+1] and then 1 to req_done[4r+2], in host
+    // memory, after a system-wide fence.
+    const uint32_t *req_of = nullptr, *req_lane0 = nullptr;
+    uint32_t *req_left = nullptr, *req_acc = nullptr, *req_done = nullptr;
+    void *const *req_out = nullptr;
 };
 
 cudaError_t launch_traj(const TrajLaunch &L, cudaStream_t stream);

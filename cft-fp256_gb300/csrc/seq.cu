@@ -422,6 +422,37 @@ __global__ void k_seq(const SeqLaunch L, size_t lane0, size_t nl)
     }
 }
 
+// A lane of an early-completing launch (TrajLaunch::req_of) has finished:
+// one thread a lane, after the lane's final block is written and fenced.
+SFD void lane_finished(const TrajLaunch &L, size_t lane, uint32_t lflags, uint32_t lstatus)
+{
+    const uint32_t r = L.req_of[lane];
+    if (lflags) atomicOr(L.req_acc + 2 * (size_t)r, lflags);
+    if (lstatus) atomicOr(L.req_acc + 2 * (size_t)r + 1, lstatus);
+    __threadfence();
+    if (atomicSub(L.req_left + r, 1u) == 1u) {                // the request's last lane
+        __threadfence();
+        const uint32_t f = atomicOr(L.req_acc + 2 * (size_t)r, 0u);
+        const uint32_t st = atomicOr(L.req_acc + 2 * (size_t)r + 1, 0u);
+        volatile uint32_t *d = L.req_done + 4 * (size_t)r;
+        d[0] = f;
+        d[1] = st;
+        __threadfence_system();
+        d[2] = 1u;
+    }
+}
+
+// The block of `slots` elements a finished lane leaves, in its request's
+// host output (TrajLaunch::req_out), or NULL.
+template <int W>
+SFD uint32_t *lane_out(const TrajLaunch &L, size_t lane, uint32_t slots)
+{
+    if (!L.req_out) return nullptr;
+    const uint32_t r = L.req_of[lane];
+    uint32_t *o = static_cast<uint32_t *>(L.req_out[r]);
+    return o ? o + (size_t)(lane - L.req_lane0[r]) * slots * W : nullptr;
+}
+
 // Trajectories: each lane runs the program `segments[lane]` times, the
 // scratch-out block of one run feeding the scratch-in block of the next
 // (n_scratch_in == n_scratch_out), every run a complete program run as
@@ -496,6 +527,21 @@ __global__ void k_traj(const TrajLaunch L, bool scratch_shared)
                         snaps[((lane * L.max_snaps + k) * slots + s) * W + w] = sc.at(s, w);
                 }
             }
+        }
+        if (L.req_of && mine && seg + 1 == segs) {            // this lane is done
+            uint32_t *ho = lane_out<W>(L, lane, slots);
+            for (uint32_t s = 0; s < slots; s++) {
+#pragma unroll
+                for (int w = 0; w < W; w++) {
+                    const uint32_t v = sc.base ? sc.at(s, w) : state[(lane * slots + s) * W + w];
+                    state[(lane * slots + s) * W + w] = v;
+                    if (ho) ho[s * W + w] = v;
+                }
+            }
+            if (L.lane_flags) L.lane_flags[lane] = lflag;
+            if (L.lane_status) L.lane_status[lane] = status;
+            __threadfence_system();
+            lane_finished(L, lane, lflag & 0x1Fu, status);
         }
     }
     if (have) {
@@ -655,6 +701,29 @@ __global__ void __launch_bounds__(32) k_traj_g(const TrajLaunch L)
                     for (int w = 0; w < W; w++)
                         snaps[((lane * L.max_snaps + k) * slots + sl) * W + w] = LOC(32 + sl, w);
                 }
+            }
+        }
+        const bool last = L.req_of && mine && seg + 1 == segs;     // this lane is done
+        if (__any_sync(0xFFFFFFFFu, last)) {
+            uint32_t lf = flags;
+            for (int o = 1; o < G; o <<= 1) lf |= __shfl_xor_sync(0xFFFFFFFFu, lf, o);
+            if (last) {
+                uint32_t *ho = lane_out<W>(L, lane, slots);
+                for (uint32_t sl = g; sl < slots; sl += G) {
+#pragma unroll
+                    for (int w = 0; w < W; w++) {
+                        const uint32_t v = LOC(32 + sl, w);
+                        state[(lane * slots + sl) * W + w] = v;
+                        if (ho) ho[sl * W + w] = v;
+                    }
+                }
+                __threadfence_system();
+            }
+            __syncwarp();
+            if (last && g == 0) {
+                if (L.lane_flags) L.lane_flags[lane] = (uint8_t)(lf & 0x1Fu);
+                if (L.lane_status) L.lane_status[lane] = 0u;
+                lane_finished(L, lane, lf & 0x1Fu, 0u);
             }
         }
     }

@@ -52,6 +52,8 @@ struct Req {
     size_t off = 0;                 // element requests: the output's arena offset
     const SeqProgram *P = nullptr;
     bool out_pinned = false;        // host_out readable by an async copy
+    void *out_dev = nullptr;        // host_out as the GPU addresses it, or NULL
+    bool early = false;             // program request completed before its batch
     uint64_t t_arrival = 0, t_admit = 0;
 };
 
@@ -70,6 +72,15 @@ struct Slot {
     uint8_t *h_lflags = nullptr, *d_lflags = nullptr;
     uint8_t *h_init = nullptr;       // pinned staging of the initial blocks
     size_t h_init_cap = 0;
+    // completion a request at a time (TrajLaunch::req_of): per lane its
+    // request; per request its first lane, lanes left, flags/STATUS and
+    // output; the done records in mapped host memory
+    uint32_t *h_req_of = nullptr, *d_req_of = nullptr;
+    uint32_t *h_req_lane0 = nullptr, *d_req_lane0 = nullptr;
+    uint32_t *h_req_left = nullptr, *d_req_left = nullptr, *d_req_acc = nullptr;
+    void **h_req_out = nullptr, **d_req_out = nullptr;
+    uint32_t *h_done = nullptr, *d_done = nullptr;
+    size_t req_cap = 0;
     size_t prog_off = 0, prog_bytes = 0;
     std::vector<Req *> reqs;
     std::vector<size_t> lane0;
@@ -112,12 +123,13 @@ struct cftg_server {
     bool launch_elem(Slot &sl);
     bool launch_prog(Slot &sl);
     void retire(Slot &sl, cudaError_t e);
+    bool early_completions(Slot &sl);
     void complete(Req *q, int32_t result, uint32_t flags, uint32_t status, uint32_t batch,
-                  uint64_t t_done);
+                  uint64_t t_done, bool release = true);
 };
 
 void cftg_server::complete(Req *q, int32_t result, uint32_t flags, uint32_t status, uint32_t batch,
-                           uint64_t t_done)
+                           uint64_t t_done, bool release)
 {
     cftg_completion c;
     memset(&c, 0, sizeof c);
@@ -135,8 +147,29 @@ void cftg_server::complete(Req *q, int32_t result, uint32_t flags, uint32_t stat
     if (result != CFT_OK) st.failed++;
     else if (q->r.type == CFTG_REQ_ELEM) st.elements_done += q->r.n;
     else st.lane_runs_done += (uint64_t)q->r.lanes * q->r.runs;
-    delete q;
+    if (release) delete q;
     cv_done.notify_all();
+}
+
+// A program request whose output the GPU writes completes when its last lane
+// has finished, not when its batch has: the trajectory kernel marks it done
+// in the slot's mapped records (TrajLaunch::req_of).
+static bool completes_early(const Req *q) { return !q->r.host_out || q->out_dev; }
+
+bool cftg_server::early_completions(Slot &sl)
+{
+    bool any = false;
+    for (size_t i = 0; i < sl.reqs.size(); i++) {
+        Req *q = sl.reqs[i];
+        if (q->early || !completes_early(q)) continue;
+        const volatile uint32_t *d = sl.h_done + 4 * i;
+        if (!d[2]) continue;
+        std::atomic_thread_fence(std::memory_order_acquire);
+        q->early = true;
+        complete(q, CFT_OK, d[0] & CFT_FLAGS_ALL, d[1], sl.id, now_ns(), false);
+        any = true;
+    }
+    return any;
 }
 
 // Element batch: requests taken from the head of elem_q while calls and
@@ -234,7 +267,7 @@ bool cftg_server::launch_prog(Slot &sl)
             ++it;
             continue;
         }
-        if (!take.empty() && (lanes + q->r.lanes > cfg.max_batch_lanes ||
+        if (!take.empty() && (lanes + q->r.lanes > cfg.max_batch_lanes || take.size() >= sl.req_cap ||
                               (lanes + q->r.lanes) * state_lane > sl.h_init_cap))
             break;
         take.push_back(q);
@@ -270,9 +303,17 @@ bool cftg_server::launch_prog(Slot &sl)
     size_t l = 0;
     for (Req *q : take) {
         q->t_admit = t;
+        const size_t ri = sl.reqs.size();
         sl.reqs.push_back(q);
         sl.lane0.push_back(l);
-        for (size_t j = 0; j < q->r.lanes; j++) sl.h_seg[l + j] = q->r.runs;
+        for (size_t j = 0; j < q->r.lanes; j++) {
+            sl.h_seg[l + j] = q->r.runs;
+            sl.h_req_of[l + j] = (uint32_t)ri;
+        }
+        sl.h_req_lane0[ri] = (uint32_t)l;
+        sl.h_req_left[ri] = (uint32_t)q->r.lanes;
+        sl.h_req_out[ri] = q->r.host_out ? q->out_dev : nullptr;
+        memset(sl.h_done + 4 * ri, 0, 4 * sizeof(uint32_t));
         if (e == cudaSuccess && !q->init.empty())
             memcpy(sl.h_init + l * P.n_scratch_out * esz, q->init.data(), q->init.size());
         l += q->r.lanes;
@@ -287,6 +328,17 @@ bool cftg_server::launch_prog(Slot &sl)
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(sl.d_order, sl.h_order, lanes * 4, cudaMemcpyHostToDevice, sl.s);
     if (e == cudaSuccess) e = cudaMemsetAsync(sl.d_word, 0, 4 * sizeof(uint32_t), sl.s);
+    const size_t nreq = sl.reqs.size();
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(sl.d_req_of, sl.h_req_of, lanes * 4, cudaMemcpyHostToDevice, sl.s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(sl.d_req_lane0, sl.h_req_lane0, nreq * 4, cudaMemcpyHostToDevice, sl.s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(sl.d_req_left, sl.h_req_left, nreq * 4, cudaMemcpyHostToDevice, sl.s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(sl.d_req_out, sl.h_req_out, nreq * sizeof(void *), cudaMemcpyHostToDevice,
+                            sl.s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(sl.d_req_acc, 0, nreq * 2 * 4, sl.s);
     TrajLaunch T;
     T.P = P;
     if (P.flags & CFT_PROG_FLAG_BANK_EXT) T.P.d_consts = head->r.d_bank;
@@ -298,6 +350,12 @@ bool cftg_server::launch_prog(Slot &sl)
     T.lane_flags = sl.d_lflags;
     T.lane_status = sl.d_lstatus;
     T.word = sl.d_word;
+    T.req_of = sl.d_req_of;
+    T.req_lane0 = sl.d_req_lane0;
+    T.req_left = sl.d_req_left;
+    T.req_acc = sl.d_req_acc;
+    T.req_done = sl.d_done;
+    T.req_out = sl.d_req_out;
     plan_lanes(head->r.prog, lanes, T);
     T.sm_regs = traj_sm_regs;
     T.sm_smem = traj_sm_smem;
@@ -310,7 +368,7 @@ bool cftg_server::launch_prog(Slot &sl)
         e = cudaMemcpyAsync(sl.h_word, sl.d_word, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, sl.s);
     for (size_t i = 0; e == cudaSuccess && i < sl.reqs.size(); i++) {
         Req *q = sl.reqs[i];
-        if (q->r.host_out && q->out_pinned)
+        if (q->r.host_out && q->out_pinned && !q->out_dev)    // the kernel writes the others
             e = cudaMemcpyAsync(q->r.host_out, state + sl.lane0[i] * P.n_scratch_out * esz,
                                 q->out_bytes, cudaMemcpyDeviceToHost, sl.s);
     }
@@ -353,8 +411,13 @@ void cftg_server::retire(Slot &sl, cudaError_t e)
     } else {
         const SeqProgram *P = sl.reqs.empty() ? nullptr : sl.reqs[0]->P;
         const bool bad = e != cudaSuccess || sl.h_word[2] != 0u;
+        if (e == cudaSuccess) early_completions(sl);     // the last ones, before any is freed
         for (size_t i = 0; i < sl.reqs.size(); i++) {
             Req *q = sl.reqs[i];
+            if (q->early) {                       // posted when its last lane finished
+                delete q;
+                continue;
+            }
             uint32_t fl = 0, stt = 0;
             for (size_t j = 0; !bad && j < q->r.lanes; j++) {
                 fl |= sl.h_lflags[sl.lane0[i] + j] & CFT_FLAGS_ALL;
@@ -400,7 +463,10 @@ void cftg_server::loop()
         for (auto &sl : slots) {
             if (!sl.busy) continue;
             const cudaError_t e = cudaEventQuery(sl.ev);
-            if (e == cudaErrorNotReady) continue;
+            if (e == cudaErrorNotReady) {
+                if (sl.program && early_completions(sl)) did = true;
+                continue;
+            }
             retire(sl, e);
             did = true;
         }
@@ -448,11 +514,13 @@ static void free_slot(Slot &sl)
     if (sl.ev) cudaEventDestroy(sl.ev);
     for (void *p : {(void *)sl.d_calls, (void *)sl.d_prefix, (void *)sl.d_counter, (void *)sl.d_flags,
                     (void *)sl.d_seg, (void *)sl.d_order, (void *)sl.d_lstatus, (void *)sl.d_word,
-                    (void *)sl.d_lflags})
+                    (void *)sl.d_lflags, (void *)sl.d_req_of, (void *)sl.d_req_lane0,
+                    (void *)sl.d_req_left, (void *)sl.d_req_acc, (void *)sl.d_req_out})
         if (p) cudaFree(p);
     for (void *p : {(void *)sl.h_calls, (void *)sl.h_prefix, (void *)sl.h_flags, (void *)sl.h_seg,
                     (void *)sl.h_order, (void *)sl.h_lstatus, (void *)sl.h_word, (void *)sl.h_lflags,
-                    (void *)sl.h_init})
+                    (void *)sl.h_init, (void *)sl.h_req_of, (void *)sl.h_req_lane0,
+                    (void *)sl.h_req_left, (void *)sl.h_req_out, (void *)sl.h_done})
         if (p) cudaFreeHost(p);
 }
 
@@ -561,6 +629,19 @@ extern "C" cft_status cftg_server_create(cft_device *dev, const cftg_server_conf
                  cudaHostAlloc(&sl.h_word, 4 * sizeof(uint32_t), 0) == cudaSuccess &&
                  cudaHostAlloc(&sl.h_init, SERVE_INIT_STAGING, 0) == cudaSuccess;
             sl.h_init_cap = SERVE_INIT_STAGING;
+            const size_t rq = std::min<size_t>(l, 65536);
+            sl.req_cap = rq;
+            ok = ok && cudaMalloc(&sl.d_req_of, l * 4) == cudaSuccess &&
+                 cudaMalloc(&sl.d_req_lane0, rq * 4) == cudaSuccess &&
+                 cudaMalloc(&sl.d_req_left, rq * 4) == cudaSuccess &&
+                 cudaMalloc(&sl.d_req_acc, rq * 8) == cudaSuccess &&
+                 cudaMalloc(&sl.d_req_out, rq * sizeof(void *)) == cudaSuccess &&
+                 cudaHostAlloc(&sl.h_req_of, l * 4, 0) == cudaSuccess &&
+                 cudaHostAlloc(&sl.h_req_lane0, rq * 4, 0) == cudaSuccess &&
+                 cudaHostAlloc(&sl.h_req_left, rq * 4, 0) == cudaSuccess &&
+                 cudaHostAlloc(&sl.h_req_out, rq * sizeof(void *), 0) == cudaSuccess &&
+                 cudaHostAlloc(&sl.h_done, rq * 16, cudaHostAllocMapped) == cudaSuccess &&
+                 cudaHostGetDevicePointer((void **)&sl.d_done, sl.h_done, 0) == cudaSuccess;
         }
     }
     if (!ok) {
@@ -647,9 +728,15 @@ extern "C" cft_status cftg_server_submit(cftg_server *s, const cftg_request *r)
                                              "server's whole budget");
     if (r->host_out) {
         cudaPointerAttributes at;
-        q->out_pinned = cudaPointerGetAttributes(&at, r->host_out) == cudaSuccess &&
-                        at.type == cudaMemoryTypeHost;
+        const bool known = cudaPointerGetAttributes(&at, r->host_out) == cudaSuccess;
         cudaGetLastError();
+        q->out_pinned = known && at.type == cudaMemoryTypeHost;
+        // where the GPU can write the caller's buffer itself: pinned memory
+        // through its mapped address, any host memory where the GPU walks
+        // the host's page tables
+        if (q->out_pinned && at.devicePointer) q->out_dev = at.devicePointer;
+        else if (known && at.type == cudaMemoryTypeUnregistered && s->dev->host_page_tables)
+            q->out_dev = r->host_out;
     }
     {
         std::lock_guard<std::mutex> g(s->mu);

@@ -197,3 +197,47 @@ def test_mixed_requests_same_alone_and_in_the_mix(gpu):
             assert not diff, f"program request {tag} ({lanes} lanes, {runs} runs): lanes {diff} differ"
             assert flags[tag] == fl and status[tag] == stt == 0, (tag, flags[tag], fl, status[tag], stt)
     L.cft_program_free(prog)
+
+
+def test_short_program_request_completes_before_its_batch(gpu):
+    """A short ensemble batched with a long one completes when its own lanes
+    have finished (its completion time is before the long one's), and both
+    results equal the same requests run alone; so does a request whose
+    output is pageable host memory (written by the kernel where the GPU
+    walks the host's page tables, else copied when its batch completes)."""
+    import torch
+    L = cftgb.lib()
+    z = np.load(su.GOLD / "odes.npz")
+    img = z["hh_image"].copy()
+    prog = ctypes.c_void_p()
+    cftgb._lib.check(L.cft_program_load(gpu, img.ctypes.data, img.size, ctypes.byref(prog)), "load")
+    bank = torch.from_numpy(z["hh_bank"].copy().view(np.int32)).cuda()
+    # lanes, runs, pinned output; the first request occupies the one program
+    # slot while the other three queue, so those three form one batch
+    plan = [(32, 60, True), (32, 2, True), (32, 120, True), (8, 3, False)]
+    reqs, outs, inits = [], [], []
+    for i, (lanes, runs, pinned) in enumerate(plan):
+        init = hh_init(lanes, 900 + i)
+        out = (torch.zeros(init.nbytes, dtype=torch.uint8, pin_memory=True) if pinned
+               else np.zeros(init.nbytes, np.uint8))
+        ptr = out.data_ptr() if pinned else out.ctypes.data
+        reqs.append(serving.Request(type=serving.REQ_PROGRAM, prog=prog, d_bank=bank.data_ptr(),
+                                    init=init.ctypes.data, lanes=lanes, runs=runs,
+                                    host_out=ptr, tag=i))
+        outs.append(out)
+        inits.append(init)
+    with serving.Server(gpu, 1 << 26, max_inflight=1, max_program_inflight=1) as srv:
+        for r in reqs:
+            assert srv.submit(r) == 0
+        assert srv.drain() == 0
+        done = srv.poll()
+    assert len(done) == 4 and (done["result"] == 0).all()
+    by = {int(d["tag"]): d for d in done}
+    assert by[1]["batch"] == by[2]["batch"] == by[3]["batch"] != by[0]["batch"]
+    assert by[1]["t_done_ns"] < by[2]["t_done_ns"]
+    for i, (lanes, runs, pinned) in enumerate(plan):
+        got = (outs[i].numpy() if pinned else outs[i]).view(np.uint32)
+        want, fl, st = traj_alone(prog, bank, inits[i], lanes, runs)
+        assert np.array_equal(got.reshape(-1), want.reshape(-1)), f"request {i}"
+        assert int(by[i]["flags"]) == fl and int(by[i]["status"]) == st
+    L.cft_program_free(prog)
