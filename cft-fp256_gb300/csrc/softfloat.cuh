@@ -93,7 +93,8 @@ SFD void unpack(const uint32_t (&x)[Fmt<FMT>::W], Unp<FMT> &u)
     if (ef == 0u) {
         if (fz) { u.cls = C_ZERO; return; }
         u.cls = C_SUB;
-        const int L = sfw::bitlen(u.m);
+        // a subnormal's leading bit is nearly always in its top word
+        const int L = u.m[W - 1] ? 32 * W - __clz(u.m[W - 1]) : sfw::bitlen(u.m);
         u.ve = F::EMIN - F::MANW + L - 1;
         sfw::shl(u.m, LB + 1 - L);
         return;
@@ -196,6 +197,15 @@ SFD void round_pack(int sign, uint32_t (&m)[N], int e, int rnd, uint32_t (&out)[
 {
     using F = Fmt<FMT>;
     constexpr int W = F::W;
+    // An exact cancellation leaves with its zero first, so that the lanes
+    // left can take the fast paths below.
+    if constexpr (ZERO) {
+        if ((m[N - 1] | m[N - 2]) == 0u && sfw::is_zero(m)) {
+            enc_zero<FMT>(out, rnd == RDN ? 1 : 0);
+            flags = 0u;
+            return;
+        }
+    }
     // Most results keep their leading bit in the top word or the one below
     // (sums without deep cancellation, quotients, roots): when every lane of
     // the warp has it there, one clz.
@@ -203,16 +213,7 @@ SFD void round_pack(int sign, uint32_t (&m)[N], int e, int rnd, uint32_t (&out)[
     int L;
     if (__all_sync(am, m[N - 1] != 0u)) L = 32 * N - __clz(m[N - 1]);
     else if (__all_sync(am, m[N - 1] == 0u && m[N - 2] != 0u)) L = 32 * (N - 1) - __clz(m[N - 2]);
-    else {
-        L = sfw::bitlen(m);
-        if constexpr (ZERO) {
-            if (L == 0) {
-                enc_zero<FMT>(out, rnd == RDN ? 1 : 0);
-                flags = 0u;
-                return;
-            }
-        }
-    }
+    else L = sfw::bitlen(m);
     const int e_norm = e + L - 1;                 // exponent of the leading bit
     sfw::shl(m, 32 * N - L);                      // leading bit to the top
 
