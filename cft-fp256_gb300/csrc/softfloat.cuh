@@ -541,28 +541,29 @@ SFD void divrem_top(const uint32_t (&X)[W], const uint32_t (&Y)[W], uint32_t (&q
         }
 #pragma unroll
         for (int j = m - 1; j >= 0; j--) {
-            const uint64_t num = ((uint64_t)u[j + n] << 32) | u[j + n - 1];
-            uint64_t qhat, rhat;
+            // the digit estimate is a word: 32 x 32-bit products below
+            uint32_t qd;
+            uint64_t rhat;
             if (u[j + n] >= vt) {
-                qhat = 0xFFFFFFFFull;
-                rhat = num - qhat * vt;
+                qd = 0xFFFFFFFFu;
+                rhat = (((uint64_t)u[j + n] << 32) | u[j + n - 1]) - 0xFFFFFFFFull * vt;
             } else {
                 uint32_t r32;
-                qhat = div_2by1(u[j + n], u[j + n - 1], vt, vinv, r32);
+                qd = div_2by1(u[j + n], u[j + n - 1], vt, vinv, r32);
                 rhat = r32;
             }
-            // at most two corrections make qhat exact or one too large
+            // at most two corrections make qd exact or one too large
             for (int k = 0; k < 2; k++) {
-                if (rhat <= 0xFFFFFFFFull && qhat * vs > ((rhat << 32) | u[j + n - 2])) {
-                    qhat--;
+                if (rhat <= 0xFFFFFFFFull && (uint64_t)qd * vs > ((rhat << 32) | u[j + n - 2])) {
+                    qd--;
                     rhat += vt;
                 }
             }
-            // u[j .. j+n] -= qhat * Y
+            // u[j .. j+n] -= qd * Y
             uint32_t carry = 0u, borrow = 0u;
 #pragma unroll
             for (int i = 0; i < n; i++) {
-                const uint64_t p = qhat * Y[i] + carry;
+                const uint64_t p = (uint64_t)qd * Y[i] + carry;
                 carry = (uint32_t)(p >> 32);
                 const uint64_t t = (uint64_t)u[i + j] - (uint32_t)p - borrow;
                 u[i + j] = (uint32_t)t;
@@ -571,7 +572,7 @@ SFD void divrem_top(const uint32_t (&X)[W], const uint32_t (&Y)[W], uint32_t (&q
             const uint64_t t = (uint64_t)u[j + n] - carry - borrow;
             u[j + n] = (uint32_t)t;
             if (t >> 63) {                        // one too large: add Y back
-                qhat--;
+                qd--;
                 uint32_t c = 0u;
 #pragma unroll
                 for (int i = 0; i < n; i++) {
@@ -581,7 +582,7 @@ SFD void divrem_top(const uint32_t (&X)[W], const uint32_t (&Y)[W], uint32_t (&q
                 }
                 u[j + n] += c;
             }
-            q[j] = (uint32_t)qhat;
+            q[j] = qd;
         }
         uint32_t o = 0u;
 #pragma unroll

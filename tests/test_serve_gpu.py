@@ -226,8 +226,13 @@ def test_short_program_request_completes_before_its_batch(gpu):
                                     host_out=ptr, tag=i))
         outs.append(out)
         inits.append(init)
+    import time
     with serving.Server(gpu, 1 << 26, max_inflight=1, max_program_inflight=1) as srv:
-        for r in reqs:
+        assert srv.submit(reqs[0]) == 0
+        t_end = time.time() + 10
+        while srv.stats()["batches"] < 1 and time.time() < t_end:   # the first is on the device
+            time.sleep(0.0005)
+        for r in reqs[1:]:
             assert srv.submit(r) == 0
         assert srv.drain() == 0
         done = srv.poll()
