@@ -50,6 +50,43 @@ template <> struct MulPtx<8> {
     }
 };
 
+// u (K words) -= t (K words); returns the borrow out (1 when u < t). One
+// borrow chain; K = N + 1 for the division's multiply-subtract.
+template <int K> struct SubPtx;
+
+template <> struct SubPtx<3> {
+    static __device__ __forceinline__ uint32_t sub(uint32_t *u, const uint32_t *t)
+    {
+        uint32_t b;
+        asm("sub.cc.u32 %0, %0, %4;\n\tsubc.cc.u32 %1, %1, %5;\n\tsubc.cc.u32 %2, %2, %6;\n\tsubc.u32 %3, 0, 0;"
+            : "+r"(u[0]), "+r"(u[1]), "+r"(u[2]), "=r"(b)
+            : "r"(t[0]), "r"(t[1]), "r"(t[2]));
+        return b & 1u;
+    }
+};
+
+template <> struct SubPtx<5> {
+    static __device__ __forceinline__ uint32_t sub(uint32_t *u, const uint32_t *t)
+    {
+        uint32_t b;
+        asm("sub.cc.u32 %0, %0, %6;\n\tsubc.cc.u32 %1, %1, %7;\n\tsubc.cc.u32 %2, %2, %8;\n\tsubc.cc.u32 %3, %3, %9;\n\tsubc.cc.u32 %4, %4, %10;\n\tsubc.u32 %5, 0, 0;"
+            : "+r"(u[0]), "+r"(u[1]), "+r"(u[2]), "+r"(u[3]), "+r"(u[4]), "=r"(b)
+            : "r"(t[0]), "r"(t[1]), "r"(t[2]), "r"(t[3]), "r"(t[4]));
+        return b & 1u;
+    }
+};
+
+template <> struct SubPtx<9> {
+    static __device__ __forceinline__ uint32_t sub(uint32_t *u, const uint32_t *t)
+    {
+        uint32_t b;
+        asm("sub.cc.u32 %0, %0, %10;\n\tsubc.cc.u32 %1, %1, %11;\n\tsubc.cc.u32 %2, %2, %12;\n\tsubc.cc.u32 %3, %3, %13;\n\tsubc.cc.u32 %4, %4, %14;\n\tsubc.cc.u32 %5, %5, %15;\n\tsubc.cc.u32 %6, %6, %16;\n\tsubc.cc.u32 %7, %7, %17;\n\tsubc.cc.u32 %8, %8, %18;\n\tsubc.u32 %9, 0, 0;"
+            : "+r"(u[0]), "+r"(u[1]), "+r"(u[2]), "+r"(u[3]), "+r"(u[4]), "+r"(u[5]), "+r"(u[6]), "+r"(u[7]), "+r"(u[8]), "=r"(b)
+            : "r"(t[0]), "r"(t[1]), "r"(t[2]), "r"(t[3]), "r"(t[4]), "r"(t[5]), "r"(t[6]), "r"(t[7]), "r"(t[8]));
+        return b & 1u;
+    }
+};
+
 // r (2N words) = a * b
 template <int N>
 __device__ __forceinline__ void mul_ptx(uint32_t (&r)[2 * N], const uint32_t (&a)[N],

@@ -559,19 +559,12 @@ SFD void divrem_top(const uint32_t (&X)[W], const uint32_t (&Y)[W], uint32_t (&q
                     rhat += vt;
                 }
             }
-            // u[j .. j+n] -= qd * Y
-            uint32_t carry = 0u, borrow = 0u;
+            // u[j .. j+n] -= qd * Y: the row on the IMAD pipe, one borrow chain
+            uint32_t row[n + 1];
 #pragma unroll
-            for (int i = 0; i < n; i++) {
-                const uint64_t p = (uint64_t)qd * Y[i] + carry;
-                carry = (uint32_t)(p >> 32);
-                const uint64_t t = (uint64_t)u[i + j] - (uint32_t)p - borrow;
-                u[i + j] = (uint32_t)t;
-                borrow = (uint32_t)(t >> 63);
-            }
-            const uint64_t t = (uint64_t)u[j + n] - carry - borrow;
-            u[j + n] = (uint32_t)t;
-            if (t >> 63) {                        // one too large: add Y back
+            for (int i = 0; i <= n; i++) row[i] = 0u;
+            sfw::MulPtx<n>::row(row, qd, Y);
+            if (sfw::SubPtx<n + 1>::sub(u + j, row)) {   // one too large: add Y back
                 qd--;
                 uint32_t c = 0u;
 #pragma unroll
