@@ -87,6 +87,62 @@ template <> struct SubPtx<9> {
     }
 };
 
+// The widths the square root's remainder takes (W + 2 words).
+template <> struct MulPtx<3> {
+    static __device__ __forceinline__ void row(uint32_t *r, uint32_t a, const uint32_t (&b)[3])
+    {
+        asm("mad.lo.cc.u32 %0, %4, %5, %0;\n\tmadc.lo.cc.u32 %1, %4, %6, %1;\n\tmadc.lo.cc.u32 %2, %4, %7, %2;\n\taddc.u32 %3, %3, 0;\n\tmad.hi.cc.u32 %1, %4, %5, %1;\n\tmadc.hi.cc.u32 %2, %4, %6, %2;\n\tmadc.hi.u32 %3, %4, %7, %3;"
+            : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3])
+            : "r"(a), "r"(b[0]), "r"(b[1]), "r"(b[2]));
+    }
+};
+template <> struct MulPtx<6> {
+    static __device__ __forceinline__ void row(uint32_t *r, uint32_t a, const uint32_t (&b)[6])
+    {
+        asm("mad.lo.cc.u32 %0, %7, %8, %0;\n\tmadc.lo.cc.u32 %1, %7, %9, %1;\n\tmadc.lo.cc.u32 %2, %7, %10, %2;\n\tmadc.lo.cc.u32 %3, %7, %11, %3;\n\tmadc.lo.cc.u32 %4, %7, %12, %4;\n\tmadc.lo.cc.u32 %5, %7, %13, %5;\n\taddc.u32 %6, %6, 0;\n\tmad.hi.cc.u32 %1, %7, %8, %1;\n\tmadc.hi.cc.u32 %2, %7, %9, %2;\n\tmadc.hi.cc.u32 %3, %7, %10, %3;\n\tmadc.hi.cc.u32 %4, %7, %11, %4;\n\tmadc.hi.cc.u32 %5, %7, %12, %5;\n\tmadc.hi.u32 %6, %7, %13, %6;"
+            : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6])
+            : "r"(a), "r"(b[0]), "r"(b[1]), "r"(b[2]), "r"(b[3]), "r"(b[4]), "r"(b[5]));
+    }
+};
+template <> struct MulPtx<10> {
+    static __device__ __forceinline__ void row(uint32_t *r, uint32_t a, const uint32_t (&b)[10])
+    {
+        asm("mad.lo.cc.u32 %0, %11, %12, %0;\n\tmadc.lo.cc.u32 %1, %11, %13, %1;\n\tmadc.lo.cc.u32 %2, %11, %14, %2;\n\tmadc.lo.cc.u32 %3, %11, %15, %3;\n\tmadc.lo.cc.u32 %4, %11, %16, %4;\n\tmadc.lo.cc.u32 %5, %11, %17, %5;\n\tmadc.lo.cc.u32 %6, %11, %18, %6;\n\tmadc.lo.cc.u32 %7, %11, %19, %7;\n\tmadc.lo.cc.u32 %8, %11, %20, %8;\n\tmadc.lo.cc.u32 %9, %11, %21, %9;\n\taddc.u32 %10, %10, 0;\n\tmad.hi.cc.u32 %1, %11, %12, %1;\n\tmadc.hi.cc.u32 %2, %11, %13, %2;\n\tmadc.hi.cc.u32 %3, %11, %14, %3;\n\tmadc.hi.cc.u32 %4, %11, %15, %4;\n\tmadc.hi.cc.u32 %5, %11, %16, %5;\n\tmadc.hi.cc.u32 %6, %11, %17, %6;\n\tmadc.hi.cc.u32 %7, %11, %18, %7;\n\tmadc.hi.cc.u32 %8, %11, %19, %8;\n\tmadc.hi.cc.u32 %9, %11, %20, %9;\n\tmadc.hi.u32 %10, %11, %21, %10;"
+            : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]), "+r"(r[8]), "+r"(r[9]), "+r"(r[10])
+            : "r"(a), "r"(b[0]), "r"(b[1]), "r"(b[2]), "r"(b[3]), "r"(b[4]), "r"(b[5]), "r"(b[6]), "r"(b[7]), "r"(b[8]), "r"(b[9]));
+    }
+};
+template <> struct SubPtx<4> {
+    static __device__ __forceinline__ uint32_t sub(uint32_t *u, const uint32_t *t)
+    {
+        uint32_t b;
+        asm("sub.cc.u32 %0, %0, %5;\n\tsubc.cc.u32 %1, %1, %6;\n\tsubc.cc.u32 %2, %2, %7;\n\tsubc.cc.u32 %3, %3, %8;\n\tsubc.u32 %4, 0, 0;"
+            : "+r"(u[0]), "+r"(u[1]), "+r"(u[2]), "+r"(u[3]), "=r"(b)
+            : "r"(t[0]), "r"(t[1]), "r"(t[2]), "r"(t[3]));
+        return b & 1u;
+    }
+};
+template <> struct SubPtx<6> {
+    static __device__ __forceinline__ uint32_t sub(uint32_t *u, const uint32_t *t)
+    {
+        uint32_t b;
+        asm("sub.cc.u32 %0, %0, %7;\n\tsubc.cc.u32 %1, %1, %8;\n\tsubc.cc.u32 %2, %2, %9;\n\tsubc.cc.u32 %3, %3, %10;\n\tsubc.cc.u32 %4, %4, %11;\n\tsubc.cc.u32 %5, %5, %12;\n\tsubc.u32 %6, 0, 0;"
+            : "+r"(u[0]), "+r"(u[1]), "+r"(u[2]), "+r"(u[3]), "+r"(u[4]), "+r"(u[5]), "=r"(b)
+            : "r"(t[0]), "r"(t[1]), "r"(t[2]), "r"(t[3]), "r"(t[4]), "r"(t[5]));
+        return b & 1u;
+    }
+};
+template <> struct SubPtx<10> {
+    static __device__ __forceinline__ uint32_t sub(uint32_t *u, const uint32_t *t)
+    {
+        uint32_t b;
+        asm("sub.cc.u32 %0, %0, %11;\n\tsubc.cc.u32 %1, %1, %12;\n\tsubc.cc.u32 %2, %2, %13;\n\tsubc.cc.u32 %3, %3, %14;\n\tsubc.cc.u32 %4, %4, %15;\n\tsubc.cc.u32 %5, %5, %16;\n\tsubc.cc.u32 %6, %6, %17;\n\tsubc.cc.u32 %7, %7, %18;\n\tsubc.cc.u32 %8, %8, %19;\n\tsubc.cc.u32 %9, %9, %20;\n\tsubc.u32 %10, 0, 0;"
+            : "+r"(u[0]), "+r"(u[1]), "+r"(u[2]), "+r"(u[3]), "+r"(u[4]), "+r"(u[5]), "+r"(u[6]), "+r"(u[7]), "+r"(u[8]), "+r"(u[9]), "=r"(b)
+            : "r"(t[0]), "r"(t[1]), "r"(t[2]), "r"(t[3]), "r"(t[4]), "r"(t[5]), "r"(t[6]), "r"(t[7]), "r"(t[8]), "r"(t[9]));
+        return b & 1u;
+    }
+};
+
 // r (2N words) = a * b
 template <int N>
 __device__ __forceinline__ void mul_ptx(uint32_t (&r)[2 * N], const uint32_t (&a)[N],

@@ -699,19 +699,15 @@ SFD void isqrtrem(const uint32_t (&N)[2 * W], uint32_t (&S)[W], uint32_t &rnz)
             const uint32_t lo = (j >= 2 && j - 2 <= W) ? r[j - 2] : 0u;
             D[j] = __funnelshift_l(lo, hi, 1);
         }
-        // rem -= D * d   (D * d < B^(i+3) <= B^RW: no carry out)
-        uint32_t carry = 0u, borrow = 0u;
+        // rem -= D * d   (D * d < B^(i+3) <= B^RW: no carry out, so the
+        // row's top word is zero): the row on the IMAD pipe, one borrow chain
+        uint32_t row[RW + 1];
 #pragma unroll
-        for (int j = 0; j < RW; j++) {
-            const uint64_t pj = (uint64_t)D[j] * d + carry;
-            carry = (uint32_t)(pj >> 32);
-            const uint64_t tj = (uint64_t)rem[j] - (uint32_t)pj - borrow;
-            rem[j] = (uint32_t)tj;
-            borrow = (uint32_t)(tj >> 63);
-        }
+        for (int j = 0; j <= RW; j++) row[j] = 0u;
+        sfw::MulPtx<RW>::row(row, d, D);
         // the estimate is never low and at most three high: while rem < 0,
         // d -= 1 and rem += 2 r B + 2 d + 1
-        bool neg = borrow != 0u;
+        bool neg = sfw::SubPtx<RW>::sub(rem, row) != 0u;
 #pragma unroll
         for (int k = 0; k < 3; k++) {
             if (neg) {
