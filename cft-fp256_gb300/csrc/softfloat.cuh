@@ -237,7 +237,10 @@ SFD void round_pack(int sign, uint32_t (&m)[N], int e, int rnd, uint32_t (&out)[
     }
     const bool inexact = guard || sticky;
     uint32_t fl = inexact ? F_INEXACT : 0u;
-    if (up) sfw::inc(kept);
+    if (up) {
+        if constexpr (W >= 2) sfw::IncPtx<W>::inc(kept);
+        else sfw::inc(kept);
+    }
 
     if (d > 0) {
         // Subnormal (or rounded up into the smallest normal, whose bits are
@@ -356,26 +359,25 @@ SFD void fma_general(const Unp<FMT> &ua, const Unp<FMT> &ub, const Unp<FMT> &uc,
         // Y + X, or Y - X in two's complement, then the magnitude.
         const bool sub = sp != sc;
         const uint32_t mk = sub ? 0xFFFFFFFFu : 0u;
-        uint32_t cy = sub ? 1u : 0u;
 #pragma unroll
         for (int i = 0; i < N; i++) {
-            const uint64_t t = (uint64_t)Y[i] + (X[i] ^ mk) + cy;
-            P[i] = (uint32_t)t;
-            cy = (uint32_t)(t >> 32);
+            P[i] = Y[i];
+            X[i] ^= mk;
         }
+        const uint32_t cy = sfw::AddPtx<N>::add(P, X, sub ? 1u : 0u);
         const bool neg = sub && !cy;               // Y < X: the result is X - Y
         // the negation only where some lane of the warp needs it (the
         // smaller-exponent term is the larger magnitude only under deep
         // cancellation)
         if (__any_sync(__activemask(), neg)) {
             const uint32_t m2 = neg ? 0xFFFFFFFFu : 0u;
-            uint32_t c2 = neg ? 1u : 0u;
+            uint32_t z[N];
 #pragma unroll
             for (int i = 0; i < N; i++) {
-                const uint64_t t = (uint64_t)(P[i] ^ m2) + c2;
-                P[i] = (uint32_t)t;
-                c2 = (uint32_t)(t >> 32);
+                P[i] ^= m2;
+                z[i] = 0u;
             }
+            sfw::AddPtx<N>::add(P, z, neg ? 1u : 0u);
         }
         rs = neg ? s_small : s_big;
     }
