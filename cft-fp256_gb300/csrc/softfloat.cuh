@@ -82,16 +82,16 @@ SFD void unpack(const uint32_t (&x)[Fmt<FMT>::W], Unp<FMT> &u)
 #pragma unroll
     for (int i = 0; i < W; i++) u.m[i] = x[i];
     u.m[W - 1] &= (1u << exp_shift<FMT>()) - 1u;          // fraction only
-    const bool fz = sfw::is_zero(u.m);
     u.snan = 0;
     u.ve = 0;
     if (ef == exp_mask<FMT>()) {
+        const bool fz = sfw::is_zero(u.m);
         u.cls = fz ? C_INF : C_NAN;
         u.snan = (!fz && !((x[(F::MANW - 1) >> 5] >> ((F::MANW - 1) & 31)) & 1u)) ? 1 : 0;
         return;
     }
     if (ef == 0u) {
-        if (fz) { u.cls = C_ZERO; return; }
+        if (sfw::is_zero(u.m)) { u.cls = C_ZERO; return; }
         u.cls = C_SUB;
         // a subnormal's leading bit is nearly always in its top word
         const int L = u.m[W - 1] ? 32 * W - __clz(u.m[W - 1]) : sfw::bitlen(u.m);
@@ -337,12 +337,8 @@ SFD void fma_general(const Unp<FMT> &ua, const Unp<FMT> &ub, const Unp<FMT> &uc,
 #pragma unroll
         for (int i = 0; i < W; i++) C[i] = 0u;
 #pragma unroll
-        for (int i = 0; i < W; i++) C[W + i] = uc.m[i];
+        for (int i = 0; i < W; i++) C[W + i] = uc.m[i];    // a zero's significand is zero
         const bool czero = uc.cls == C_ZERO;
-        if (czero) {
-#pragma unroll
-            for (int i = W; i < N; i++) C[i] = 0u;
-        }
         // Branch-free alignment: Y keeps its place, X (the term with the
         // smaller exponent) is shifted right by |delta| with jamming.
         const int delta = czero ? -(1 << 28) : uc.ve - (ew + 64 * W - 2);
