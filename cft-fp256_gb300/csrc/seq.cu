@@ -463,7 +463,10 @@ SFD uint32_t *lane_out(const TrajLaunch &L, size_t lane, uint32_t slots)
 // warp's runs. Every `snap_every` runs the carried block is copied to the
 // lane's snapshot list. Flags, STATUS and the lane byte are ORed over runs
 // (STATUS also per lane when lane_status is given). A NULL a stream reads +0.
-template <int FMT>
+// EARLY: the launch completes requests as their lanes finish
+// (TrajLaunch::req_of); a separate instantiation, since the code for it
+// costs the plain launches a few per cent even when it does not run.
+template <int FMT, bool EARLY>
 __global__ void k_traj(const TrajLaunch L, bool scratch_shared)
 {
     constexpr int W = sf::Fmt<FMT>::W;
@@ -528,7 +531,7 @@ __global__ void k_traj(const TrajLaunch L, bool scratch_shared)
                 }
             }
         }
-        if (L.req_of && mine && seg + 1 == segs) {            // this lane is done
+        if (EARLY && mine && seg + 1 == segs) {               // this lane is done
             uint32_t *ho = lane_out<W>(L, lane, slots);
             for (uint32_t s = 0; s < slots; s++) {
 #pragma unroll
@@ -575,7 +578,7 @@ __global__ void k_traj(const TrajLaunch L, bool scratch_shared)
 // programs without deposits, lane-mask changes, indexed scratch, quiet
 // regions or raises are scheduled, so the lane byte holds the IEEE flags
 // alone and STATUS stays 0.
-template <int FMT>
+template <int FMT, bool EARLY>
 __global__ void __launch_bounds__(32) k_traj_g(const TrajLaunch L)
 {
     constexpr int W = sf::Fmt<FMT>::W;
@@ -703,8 +706,8 @@ __global__ void __launch_bounds__(32) k_traj_g(const TrajLaunch L)
                 }
             }
         }
-        const bool last = L.req_of && mine && seg + 1 == segs;     // this lane is done
-        if (__any_sync(0xFFFFFFFFu, last)) {
+        const bool last = EARLY && mine && seg + 1 == segs;        // this lane is done
+        if (EARLY && __any_sync(0xFFFFFFFFu, last)) {
             uint32_t lf = flags;
             for (int o = 1; o < G; o <<= 1) lf |= __shfl_xor_sync(0xFFFFFFFFu, lf, o);
             if (last) {
@@ -826,12 +829,20 @@ static cudaError_t go_traj(const TrajLaunch &L, cudaStream_t s)
     const size_t scr = (size_t)L.P.reach * W * 4;
     const bool shared = L.P.reach > 0 && (regs + scr) * T <= (160u << 10);
     if (shared) smem += scr * T;
-    smem = capped_smem(k_traj<FMT>, L, T, smem);
-    static unsigned done = 0;
-    cudaError_t e = smem_ceiling_once(k_traj<FMT>, done);
-    if (e != cudaSuccess) return e;
     const size_t blocks = (L.n + T - 1) / T;
-    k_traj<FMT><<<(unsigned)blocks, T, smem, s>>>(L, shared);
+    if (L.req_of) {
+        smem = capped_smem(k_traj<FMT, true>, L, T, smem);
+        static unsigned done = 0;
+        cudaError_t e = smem_ceiling_once(k_traj<FMT, true>, done);
+        if (e != cudaSuccess) return e;
+        k_traj<FMT, true><<<(unsigned)blocks, T, smem, s>>>(L, shared);
+    } else {
+        smem = capped_smem(k_traj<FMT, false>, L, T, smem);
+        static unsigned done = 0;
+        cudaError_t e = smem_ceiling_once(k_traj<FMT, false>, done);
+        if (e != cudaSuccess) return e;
+        k_traj<FMT, false><<<(unsigned)blocks, T, smem, s>>>(L, shared);
+    }
     return cudaGetLastError();
 }
 
@@ -840,12 +851,21 @@ static cudaError_t go_traj_g(const TrajLaunch &L, cudaStream_t s)
 {
     constexpr int W = sf::Fmt<FMT>::W;
     const int LPB = 32 / L.G;
-    const size_t smem = capped_smem(k_traj_g<FMT>, L, 32, (size_t)L.nloc * (size_t)(W * LPB + 1) * 4);
-    static unsigned done = 0;
-    cudaError_t e = smem_ceiling_once(k_traj_g<FMT>, done);
-    if (e != cudaSuccess) return e;
+    const size_t need = (size_t)L.nloc * (size_t)(W * LPB + 1) * 4;
     const size_t blocks = (L.n + LPB - 1) / LPB;
-    k_traj_g<FMT><<<(unsigned)blocks, 32, smem, s>>>(L);
+    if (L.req_of) {
+        const size_t smem = capped_smem(k_traj_g<FMT, true>, L, 32, need);
+        static unsigned done = 0;
+        cudaError_t e = smem_ceiling_once(k_traj_g<FMT, true>, done);
+        if (e != cudaSuccess) return e;
+        k_traj_g<FMT, true><<<(unsigned)blocks, 32, smem, s>>>(L);
+    } else {
+        const size_t smem = capped_smem(k_traj_g<FMT, false>, L, 32, need);
+        static unsigned done = 0;
+        cudaError_t e = smem_ceiling_once(k_traj_g<FMT, false>, done);
+        if (e != cudaSuccess) return e;
+        k_traj_g<FMT, false><<<(unsigned)blocks, 32, smem, s>>>(L);
+    }
     return cudaGetLastError();
 }
 
