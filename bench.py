@@ -48,8 +48,8 @@ METRIC = "fp256/fp128 FMA Gelem/s bit-exact (plain vs batched); mixed-load p50/p
 # bench.py --suite link measures it)
 LINK_READ_GBS = 211.0
 # DRAM bytes (read + write) an element of the FMA kernel, from the ncu
-# capture summarised in profiles/k_elem_fma256_n4M.md (518.3 MB / 4,194,304)
-TRAFFIC_B_PER_ELEM = {3: 518.3e6 / 4194304}
+# capture summarised in profiles/k_elem_fma256_n4M.md (402.7 + 112.7 MB / 4,194,304)
+TRAFFIC_B_PER_ELEM = {3: 515.4e6 / 4194304}
 N_DEFAULT = 1 << 24
 
 
