@@ -43,7 +43,7 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT / "cft-fp256_gb300"))
 
 METRIC = "fp256/fp128 FMA Gelem/s bit-exact (plain vs batched); mixed-load p50/p99 latency"
-# GPU reads of pinned host memory, GB/s, on this machine's GB300 hosts (the
+# GPU reads of pinned host memory, GB/s, on a GB300 with a Grace host (the
 # copy engines' host-to-device rate and a streaming kernel's, which agree;
 # bench.py --suite link measures it)
 LINK_READ_GBS = 211.0
