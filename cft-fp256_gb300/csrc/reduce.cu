@@ -9,9 +9,13 @@
 // order from the highest bit down - and each perfect subtree is the plain
 // pairwise tree over its items. That is what this file computes:
 //
-//  * k_red_chunks: one CTA a chunk of RC = 2048 items, the chunk's perfect
-//    subtree (8 items a thread as a register tree, then the 256 threads'
-//    values pairwise through shared memory). Blocks of 2^k >= RC items are
+//  * k_red_chunks: one CTA a chunk of RC = 8192 items, the chunk's perfect
+//    subtree: 32 consecutive items a thread folded by a binary counter whose
+//    five partial results stay in registers (the pairwise tree over the 32,
+//    node by node in index order), then the 256 threads' values pairwise -
+//    by shuffles inside a warp, through shared memory across warps. More
+//    items a thread keep more of the adds at full width: the levels across
+//    threads run with fewer and fewer lanes busy. Blocks of 2^k >= RC items are
 //    made of whole, aligned chunks, so the chunk results of one level form
 //    the next level's items, and the same bits-of-n structure repeats there.
 //  * k_red_final: one CTA folds everything else right to left: at every
@@ -36,7 +40,8 @@ namespace cftg {
 namespace {
 
 constexpr int RT = 256;           // threads a CTA
-constexpr int RE = 8;             // items a thread in a chunk
+constexpr int RE = 32;            // items a thread in a chunk
+constexpr int RL = 5;             // log2(RE): the fold's partial results
 constexpr uint32_t RC = RT * RE;  // items a chunk
 
 template <int W>
@@ -111,6 +116,72 @@ SFD void comb(uint32_t *l, const uint32_t *r, int rnd, uint32_t &fl)
     comb_n<FMT, MODE == RED_MAX>(l, r, rnd, &fl);
 }
 
+// The same node on values: arguments and result in registers (a call, not
+// inlined, so a fully unrolled fold stays small).
+template <int W> struct Val {
+    uint32_t w[W];
+};
+template <int W> struct ValF {
+    uint32_t w[W];
+    uint32_t f;
+};
+
+template <int FMT, bool MAX>
+__device__ __noinline__ ValF<sf::Fmt<FMT>::W> comb_v(const Val<sf::Fmt<FMT>::W> l,
+                                                     const Val<sf::Fmt<FMT>::W> r, int rnd)
+{
+    constexpr int W = sf::Fmt<FMT>::W;
+    uint32_t x[W], y[W], z[W];
+    ValF<W> o;
+    o.f = 0u;
+#pragma unroll
+    for (int w = 0; w < W; w++) {
+        x[w] = l.w[w];
+        y[w] = r.w[w];
+        z[w] = 0u;
+    }
+    if constexpr (MAX) sf::simple<FMT>(8, x, y, z, o.w, o.f);
+    else sf::arith<FMT, sf::OP_ADD>(x, z, y, rnd, o.w, o.f);
+    return o;
+}
+
+template <int FMT>
+__device__ __noinline__ ValF<sf::Fmt<FMT>::W> mul_v(const Val<sf::Fmt<FMT>::W> x,
+                                                    const Val<sf::Fmt<FMT>::W> y, int rnd)
+{
+    constexpr int W = sf::Fmt<FMT>::W;
+    uint32_t a[W], b[W], z[W];
+    ValF<W> o;
+    o.f = 0u;
+#pragma unroll
+    for (int w = 0; w < W; w++) {
+        a[w] = x.w[w];
+        b[w] = y.w[w];
+        z[w] = 0u;
+    }
+    sf::arith<FMT, sf::OP_MUL>(a, b, z, rnd, o.w, o.f);
+    return o;
+}
+
+// 9.4's rule notes an infinity (bit 0) or a signalling NaN (bit 1) among the
+// raw elements of SUMSQ and SUMABS.
+template <int FMT>
+SFD void note_special(const uint32_t (&v)[sf::Fmt<FMT>::W], uint32_t &seen)
+{
+    constexpr int W = sf::Fmt<FMT>::W;
+    constexpr int ES = sf::exp_shift<FMT>();
+    constexpr uint32_t EM = sf::exp_mask<FMT>();
+    if (((v[W - 1] >> ES) & EM) == EM) {
+        uint32_t frac = v[W - 1] & ((1u << ES) - 1u);
+#pragma unroll
+        for (int w = 0; w < W - 1; w++) frac |= v[w];
+        const int qbit = sf::Fmt<FMT>::MANW - 1;
+        const bool quiet = (v[qbit >> 5] >> (qbit & 31)) & 1u;
+        if (!frac) seen |= 1u;
+        else if (!quiet) seen |= 2u;
+    }
+}
+
 // One item into x: a leaf at level 0, a stored partial result above it.
 template <int FMT, int MODE, bool LEAF>
 SFD void item(const void *a, const void *b, size_t i, int rnd, uint32_t *x, uint32_t &fl,
@@ -119,19 +190,7 @@ SFD void item(const void *a, const void *b, size_t i, int rnd, uint32_t *x, uint
     constexpr int W = sf::Fmt<FMT>::W;
     uint32_t v[W];
     rload<W>(a, i, v);
-    if constexpr (LEAF && (MODE == RED_SQ || MODE == RED_ABS)) {
-        constexpr int ES = sf::exp_shift<FMT>();
-        constexpr uint32_t EM = sf::exp_mask<FMT>();
-        if (((v[W - 1] >> ES) & EM) == EM) {
-            uint32_t frac = v[W - 1] & ((1u << ES) - 1u);
-#pragma unroll
-            for (int w = 0; w < W - 1; w++) frac |= v[w];
-            const int qbit = sf::Fmt<FMT>::MANW - 1;
-            const bool quiet = (v[qbit >> 5] >> (qbit & 31)) & 1u;
-            if (!frac) seen |= 1u;
-            else if (!quiet) seen |= 2u;
-        }
-    }
+    if constexpr (LEAF && (MODE == RED_SQ || MODE == RED_ABS)) note_special<FMT>(v, seen);
     if constexpr (LEAF && MODE == RED_ABS) v[W - 1] &= 0x7FFFFFFFu;
 #pragma unroll
     for (int w = 0; w < W; w++) x[w] = v[w];
@@ -143,6 +202,27 @@ SFD void item(const void *a, const void *b, size_t i, int rnd, uint32_t *x, uint
             for (int w = 0; w < W; w++) y[w] = v[w];
         }
         mul_n<FMT>(x, y, rnd, &fl);
+    }
+}
+
+// item() with the leaf product through mul_v (registers, not memory).
+template <int FMT, int MODE, bool LEAF>
+SFD void item_v(const void *a, const void *b, size_t i, int rnd, uint32_t (&x)[sf::Fmt<FMT>::W],
+                uint32_t &fl, uint32_t &seen)
+{
+    constexpr int W = sf::Fmt<FMT>::W;
+    if constexpr (LEAF && (MODE == RED_DOT || MODE == RED_SQ)) {
+        Val<W> p, q;
+        rload<W>(a, i, p.w);
+        if constexpr (MODE == RED_SQ) note_special<FMT>(p.w, seen);
+        if constexpr (MODE == RED_DOT) rload<W>(b, i, q.w);
+        else q = p;
+        const ValF<W> o = mul_v<FMT>(p, q, rnd);
+#pragma unroll
+        for (int w = 0; w < W; w++) x[w] = o.w[w];
+        fl |= o.f;
+    } else {
+        item<FMT, MODE, LEAF>(a, b, i, rnd, x, fl, seen);
     }
 }
 
@@ -159,7 +239,32 @@ SFD void cta_perfect(const void *a, const void *b, size_t base, uint32_t count, 
     const uint32_t E = count >= (uint32_t)RT ? count / RT : 1u;
     const uint32_t P = count >= (uint32_t)RT ? (uint32_t)RT : count;
     const bool have = t < P;
-    if (have) {
+    if (have && E == (uint32_t)RE) {
+        // a full chunk: the binary counter over RE items, unrolled, so the
+        // pending left subtrees of each level are registers
+        Val<W> stk[RL], cur;
+        const size_t i0 = base + (size_t)t * RE;
+#pragma unroll
+        for (int k = 0; k < RE; k++) {
+            uint32_t x[W];
+            item_v<FMT, MODE, LEAF>(a, b, i0 + k, rnd, x, fl, seen);
+#pragma unroll
+            for (int w = 0; w < W; w++) cur.w[w] = x[w];
+#pragma unroll
+            for (int lev = 0; lev < RL; lev++) {
+                if (!((k >> lev) & 1)) {
+                    stk[lev] = cur;
+                    break;
+                }
+                const ValF<W> o = comb_v<FMT, MODE == RED_MAX>(stk[lev], cur, rnd);
+#pragma unroll
+                for (int w = 0; w < W; w++) cur.w[w] = o.w[w];
+                fl |= o.f;
+            }
+        }
+#pragma unroll
+        for (int w = 0; w < W; w++) v[w] = cur.w[w];
+    } else if (have) {
         uint32_t vals[RE][W];
         const size_t i0 = base + (size_t)t * E;
         for (uint32_t k = 0; k < E; k++) item<FMT, MODE, LEAF>(a, b, i0 + k, rnd, vals[k], fl, seen);
