@@ -291,13 +291,19 @@ def run_reduce(h, suites, args):
     o = oracle_lib.Oracle()
     vp, i, sz = ctypes.c_void_p, ctypes.c_int, ctypes.c_size_t
     o.L.sfp_reduce.argtypes = [i, i, i, vp, vp, vp, sz, ctypes.POINTER(ctypes.c_uint32)]
+    o.L.sfp_reduce_seg.argtypes = [i, i, i, vp, vp, vp, sz, sz, ctypes.POINTER(ctypes.c_uint32)]
     bad = 0
     for ck in checks:
         d = np.zeros_like(ck["d"])
         fl = ctypes.c_uint32()
         n = ck["a"].shape[0]
-        assert o.L.sfp_reduce(ck["fmt"], ck["op"], 0, ck["a"].ctypes.data, ck["b"].ctypes.data,
-                              d.ctypes.data, n, ctypes.byref(fl)) == 0
+        if ck["seg"] == n:
+            st = o.L.sfp_reduce(ck["fmt"], ck["op"], 0, ck["a"].ctypes.data, ck["b"].ctypes.data,
+                                d.ctypes.data, n, ctypes.byref(fl))
+        else:
+            st = o.L.sfp_reduce_seg(ck["fmt"], ck["op"], 0, ck["a"].ctypes.data, ck["b"].ctypes.data,
+                                    d.ctypes.data, n, ck["seg"], ctypes.byref(fl))
+        assert st == 0
         bad += int(not np.array_equal(d, ck["d"]) or fl.value != ck["flags"])
     res["oracle_cells_checked"] = len(checks)
     res["oracle_mismatches"] = bad

@@ -586,11 +586,13 @@ def _traj_alone(L, prog, bank, init, lanes, runs):
 RED_OPS = (("sum", 24), ("dot", 25), ("sumsq", 28), ("sumabs", 29), ("maxall", 31))
 
 
-def reduce(h, n=1 << 24, reps=3, check_n=65536, seed=17):
+def reduce(h, n=1 << 24, reps=3, check_n=65536, seed=17, seg_sizes=(1024, 65536)):
     """The reductions over n device-resident elements a format (normals with
-    exponents in [-20, 20], no specials, so the sums stay finite), timed with
-    CUDA events; the first check_n elements are reduced again and returned
-    with their operands for the oracle."""
+    exponents in [-20, 20], no specials, so the sums stay finite), and the
+    segmented SUM over segments of each of seg_sizes at binary128 and
+    binary256, timed with CUDA events; the first check_n elements (whole
+    segments of them) are reduced again and returned with their operands
+    for the oracle."""
     import torch
     from . import workload as wl
     L = _lib.lib()
@@ -632,10 +634,37 @@ def reduce(h, n=1 << 24, reps=3, check_n=65536, seed=17):
                           "gelem_s": n / ms / 1e6})
             go(check_n)
             torch.cuda.synchronize()
-            checks.append(dict(fmt=fmt, op=op, d=out.cpu().numpy().view(np.uint32).copy(),
+            checks.append(dict(fmt=fmt, op=op, seg=check_n, d=out.cpu().numpy().view(np.uint32).copy(),
                                flags=int(word[0].item()) & 0x1F,
                                a=a[:check_n * W].cpu().numpy().view(np.uint32).reshape(-1, W),
                                b=b[:check_n * W].cpu().numpy().view(np.uint32).reshape(-1, W)))
+        # the segmented form: SUM over consecutive segments of `seg` elements
+        if fmt >= 2:
+            for seg in seg_sizes:
+                outs = torch.zeros((n // seg) * W, dtype=torch.int32, device="cuda")
+
+                def gs(nn):
+                    _lib.check(L.cftg_reduce_device(h, 24, fmt, 0, a.data_ptr(), b.data_ptr(),
+                                                    outs.data_ptr(), nn, seg, part.data_ptr(),
+                                                    word.data_ptr(), s), "cftg_reduce_device")
+                gs(n)
+                torch.cuda.synchronize()
+                e0.record(stream)
+                for _ in range(reps):
+                    gs(n)
+                e1.record(stream)
+                torch.cuda.synchronize()
+                ms = e0.elapsed_time(e1) / reps
+                cells.append({"fmt": ("fp32", "fp64", "fp128", "fp256")[fmt], "op": "sum",
+                              "seg": seg, "ms": ms, "gelem_s": n / ms / 1e6})
+                cn = max(seg, check_n - check_n % seg)
+                gs(cn)
+                torch.cuda.synchronize()
+                checks.append(dict(fmt=fmt, op=24, seg=seg,
+                                   d=outs[:(cn // seg) * W].cpu().numpy().view(np.uint32).copy(),
+                                   flags=int(word[0].item()) & 0x1F,
+                                   a=a[:cn * W].cpu().numpy().view(np.uint32).reshape(-1, W),
+                                   b=b[:cn * W].cpu().numpy().view(np.uint32).reshape(-1, W)))
     return {"suite": "reduce", "elements": n, "cells": cells, "_checks": checks}
 
 

@@ -23,7 +23,8 @@
 //    chunk), lowest level first, each block's perfect subtree computed by
 //    the whole CTA, then the last level's items.
 //  * k_red_seg: the segmented form, one CTA a segment: chunks in order with
-//    a binary counter of completed perfect blocks, then the tail, folded.
+//    a binary counter of completed perfect blocks, then the tail, folded;
+//    k_red_seg_w: segments of at most 1,024 items, one warp a segment.
 //
 // Leaves: SUM the element; DOT the rounded product a*b; SUMSQ a*a; SUMABS
 // |a| (clearing the sign signals nothing); MAXALL the element, combined by
@@ -72,52 +73,10 @@ SFD void rstore(void *p, size_t i, const uint32_t (&x)[W])
     for (int w = 0; w < W; w++) q[w] = x[w];
 }
 
-// The node and leaf arithmetic, compiled once a format (not inlined at
-// every node of every tree: a binary256 add is thousands of instructions).
-template <int FMT, bool MAX>
-__device__ __noinline__ void comb_n(uint32_t *l, const uint32_t *r, int rnd, uint32_t *fl)
-{
-    constexpr int W = sf::Fmt<FMT>::W;
-    uint32_t x[W], y[W], z[W], o[W], f = 0u;
-#pragma unroll
-    for (int w = 0; w < W; w++) {
-        x[w] = l[w];
-        y[w] = r[w];
-        z[w] = 0u;
-    }
-    if constexpr (MAX) sf::simple<FMT>(8, x, y, z, o, f);
-    else sf::arith<FMT, sf::OP_ADD>(x, z, y, rnd, o, f);
-#pragma unroll
-    for (int w = 0; w < W; w++) l[w] = o[w];
-    *fl |= f;
-}
-
-template <int FMT>
-__device__ __noinline__ void mul_n(uint32_t *x, const uint32_t *yv, int rnd, uint32_t *fl)
-{
-    constexpr int W = sf::Fmt<FMT>::W;
-    uint32_t a[W], y[W], z[W], o[W], f = 0u;
-#pragma unroll
-    for (int w = 0; w < W; w++) {
-        a[w] = x[w];
-        y[w] = yv[w];
-        z[w] = 0u;
-    }
-    sf::arith<FMT, sf::OP_MUL>(a, y, z, rnd, o, f);
-#pragma unroll
-    for (int w = 0; w < W; w++) x[w] = o[w];
-    *fl |= f;
-}
-
-// A node: ADD(left, right) - the right subtree in ADD's c operand - or MAX.
-template <int FMT, int MODE>
-SFD void comb(uint32_t *l, const uint32_t *r, int rnd, uint32_t &fl)
-{
-    comb_n<FMT, MODE == RED_MAX>(l, r, rnd, &fl);
-}
-
-// The same node on values: arguments and result in registers (a call, not
-// inlined, so a fully unrolled fold stays small).
+// A node: ADD(left, right) - the right subtree in ADD's c operand - or MAX;
+// arguments and result in registers, the arithmetic a call (compiled once
+// a format, not inlined at every node: a binary256 add is a thousand
+// instructions).
 template <int W> struct Val {
     uint32_t w[W];
 };
@@ -163,6 +122,23 @@ __device__ __noinline__ ValF<sf::Fmt<FMT>::W> mul_v(const Val<sf::Fmt<FMT>::W> x
     return o;
 }
 
+template <int FMT, int MODE>
+SFD void comb(uint32_t (&l)[sf::Fmt<FMT>::W], const uint32_t (&r)[sf::Fmt<FMT>::W], int rnd,
+              uint32_t &fl)
+{
+    constexpr int W = sf::Fmt<FMT>::W;
+    Val<W> x, y;
+#pragma unroll
+    for (int w = 0; w < W; w++) {
+        x.w[w] = l[w];
+        y.w[w] = r[w];
+    }
+    const ValF<W> o = comb_v<FMT, MODE == RED_MAX>(x, y, rnd);
+#pragma unroll
+    for (int w = 0; w < W; w++) l[w] = o.w[w];
+    fl |= o.f;
+}
+
 // 9.4's rule notes an infinity (bit 0) or a signalling NaN (bit 1) among the
 // raw elements of SUMSQ and SUMABS.
 template <int FMT>
@@ -182,10 +158,11 @@ SFD void note_special(const uint32_t (&v)[sf::Fmt<FMT>::W], uint32_t &seen)
     }
 }
 
-// One item into x: a leaf at level 0, a stored partial result above it.
+// One item into x: a leaf at level 0 (SUM, SUMABS, MAXALL; the product
+// leaves are item_v's), a stored partial result above it.
 template <int FMT, int MODE, bool LEAF>
-SFD void item(const void *a, const void *b, size_t i, int rnd, uint32_t *x, uint32_t &fl,
-              uint32_t &seen)
+SFD void item(const void *a, const void *b, size_t i, int rnd, uint32_t (&x)[sf::Fmt<FMT>::W],
+              uint32_t &fl, uint32_t &seen)
 {
     constexpr int W = sf::Fmt<FMT>::W;
     uint32_t v[W];
@@ -194,15 +171,6 @@ SFD void item(const void *a, const void *b, size_t i, int rnd, uint32_t *x, uint
     if constexpr (LEAF && MODE == RED_ABS) v[W - 1] &= 0x7FFFFFFFu;
 #pragma unroll
     for (int w = 0; w < W; w++) x[w] = v[w];
-    if constexpr (LEAF && (MODE == RED_DOT || MODE == RED_SQ)) {
-        uint32_t y[W];
-        if constexpr (MODE == RED_DOT) rload<W>(b, i, y);
-        else {
-#pragma unroll
-            for (int w = 0; w < W; w++) y[w] = v[w];
-        }
-        mul_n<FMT>(x, y, rnd, &fl);
-    }
 }
 
 // item() with the leaf product through mul_v (registers, not memory).
@@ -226,26 +194,19 @@ SFD void item_v(const void *a, const void *b, size_t i, int rnd, uint32_t (&x)[s
     }
 }
 
-// The perfect subtree over `count` items (a power of two, 1..RC) from item
-// `base`, by the whole CTA; the result in thread 0's v. Each thread first
-// reduces E = count/RT consecutive items pairwise, then the threads' values
-// pair up through shared memory. sm: RT x W words.
+// The pairwise tree over E consecutive items from item i0 (E a power of two,
+// 1..RE) by one thread: a binary counter, unrolled with its steps past E
+// skipped (E is the same across the CTA or warp), so the pending left
+// subtrees of each level are registers; each node is a by-value call.
 template <int FMT, int MODE, bool LEAF>
-SFD void cta_perfect(const void *a, const void *b, size_t base, uint32_t count, int rnd,
-                     uint32_t (&v)[sf::Fmt<FMT>::W], uint32_t &fl, uint32_t &seen, uint32_t *sm)
+SFD void thread_fold(const void *a, const void *b, size_t i0, uint32_t E, int rnd,
+                     uint32_t (&v)[sf::Fmt<FMT>::W], uint32_t &fl, uint32_t &seen)
 {
     constexpr int W = sf::Fmt<FMT>::W;
-    const uint32_t t = threadIdx.x;
-    const uint32_t E = count >= (uint32_t)RT ? count / RT : 1u;
-    const uint32_t P = count >= (uint32_t)RT ? (uint32_t)RT : count;
-    const bool have = t < P;
-    if (have && E == (uint32_t)RE) {
-        // a full chunk: the binary counter over RE items, unrolled, so the
-        // pending left subtrees of each level are registers
-        Val<W> stk[RL], cur;
-        const size_t i0 = base + (size_t)t * RE;
+    Val<W> stk[RL], cur;
 #pragma unroll
-        for (int k = 0; k < RE; k++) {
+    for (int k = 0; k < RE; k++) {
+        if ((uint32_t)k < E) {
             uint32_t x[W];
             item_v<FMT, MODE, LEAF>(a, b, i0 + k, rnd, x, fl, seen);
 #pragma unroll
@@ -262,17 +223,25 @@ SFD void cta_perfect(const void *a, const void *b, size_t base, uint32_t count, 
                 fl |= o.f;
             }
         }
-#pragma unroll
-        for (int w = 0; w < W; w++) v[w] = cur.w[w];
-    } else if (have) {
-        uint32_t vals[RE][W];
-        const size_t i0 = base + (size_t)t * E;
-        for (uint32_t k = 0; k < E; k++) item<FMT, MODE, LEAF>(a, b, i0 + k, rnd, vals[k], fl, seen);
-        for (uint32_t s = 1; s < E; s <<= 1)
-            for (uint32_t i = 0; i < E; i += 2 * s) comb<FMT, MODE>(vals[i], vals[i + s], rnd, fl);
-#pragma unroll
-        for (int w = 0; w < W; w++) v[w] = vals[0][w];
     }
+#pragma unroll
+    for (int w = 0; w < W; w++) v[w] = cur.w[w];
+}
+
+// The perfect subtree over `count` items (a power of two, 1..RC) from item
+// `base`, by the whole CTA; the result in thread 0's v. Each thread first
+// reduces E = count/RT consecutive items pairwise, then the threads' values
+// pair up through shared memory. sm: RT x W words.
+template <int FMT, int MODE, bool LEAF>
+SFD void cta_perfect(const void *a, const void *b, size_t base, uint32_t count, int rnd,
+                     uint32_t (&v)[sf::Fmt<FMT>::W], uint32_t &fl, uint32_t &seen, uint32_t *sm)
+{
+    constexpr int W = sf::Fmt<FMT>::W;
+    const uint32_t t = threadIdx.x;
+    const uint32_t E = count >= (uint32_t)RT ? count / RT : 1u;
+    const uint32_t P = count >= (uint32_t)RT ? (uint32_t)RT : count;
+    const bool have = t < P;
+    if (have) thread_fold<FMT, MODE, LEAF>(a, b, base + (size_t)t * E, E, rnd, v, fl, seen);
     // the levels inside a warp by shuffles (no block barrier), the rest
     // through shared memory
     const uint32_t Pw = P < 32u ? P : 32u;
@@ -473,6 +442,60 @@ __global__ void __launch_bounds__(RT) k_red_seg(const void *a, const void *b, si
     }
 }
 
+// Segments of at most RSW elements: one warp a segment, so a thread folds up
+// to 32 items of a 1,024-item block and only five levels run across lanes.
+// Blocks of the segment's set bits, right to left as in k_red_seg.
+constexpr size_t RSW = 1024;
+
+template <int FMT, int MODE>
+__global__ void __launch_bounds__(RT) k_red_seg_w(const void *a, const void *b, size_t nseg,
+                                                  size_t seg, void *out, int rnd, uint32_t *word)
+{
+    constexpr int W = sf::Fmt<FMT>::W;
+    const uint32_t lane = threadIdx.x & 31u;
+    const size_t warps = (size_t)gridDim.x * (RT / 32);
+    uint32_t wfl = 0u;
+    for (size_t g = (size_t)blockIdx.x * (RT / 32) + threadIdx.x / 32; g < nseg; g += warps) {
+        uint32_t fl = 0u, seen = 0u, S[W];
+        bool have = false;
+        const size_t base = g * seg;
+        for (int k = 0; k <= 10; k++) {
+            if (!((seg >> k) & 1u)) continue;
+            const size_t start = base + (seg & ~(((size_t)2 << k) - 1u));
+            const uint32_t cnt = 1u << k;
+            const uint32_t P = cnt < 32u ? cnt : 32u, E = cnt / P;
+            uint32_t v[W];
+#pragma unroll
+            for (int w = 0; w < W; w++) v[w] = 0u;
+            if (lane < P) thread_fold<FMT, MODE, true>(a, b, start + (size_t)lane * E, E, rnd, v, fl, seen);
+            for (uint32_t st = 1; st < P; st <<= 1) {
+                uint32_t r[W];
+#pragma unroll
+                for (int w = 0; w < W; w++) r[w] = __shfl_down_sync(0xFFFFFFFFu, v[w], st);
+                if (lane < P && (lane & (2 * st - 1)) == 0) comb<FMT, MODE>(v, r, rnd, fl);
+            }
+            if (lane == 0) {
+                if (have) comb<FMT, MODE>(v, S, rnd, fl);          // v is the LEFT block
+#pragma unroll
+                for (int w = 0; w < W; w++) S[w] = v[w];
+                have = true;
+            }
+        }
+        fl = __reduce_or_sync(0xFFFFFFFFu, fl);
+        seen = __reduce_or_sync(0xFFFFFFFFu, seen);
+        if (lane == 0) {
+            if (!have) {
+#pragma unroll
+                for (int w = 0; w < W; w++) S[w] = 0u;
+            }
+            inf_rule<FMT, MODE>(S, fl, seen);
+            rstore<W>(out, g, S);
+            wfl |= fl;
+        }
+    }
+    if (lane == 0 && wfl) atomicOr(word, wfl);
+}
+
 int red_blocks(size_t want)
 {
     const size_t cap = (size_t)sm_count() * 4;
@@ -518,7 +541,11 @@ cudaError_t go_seg(const void *a, const void *b, size_t nseg, size_t seg, void *
 {
     cudaError_t e = cudaMemsetAsync(word, 0, sizeof(uint32_t), s);
     if (e != cudaSuccess) return e;
-    k_red_seg<FMT, MODE><<<red_blocks(nseg), RT, 0, s>>>(a, b, nseg, seg, out, rnd, word);
+    if (seg <= RSW)
+        k_red_seg_w<FMT, MODE><<<red_blocks((nseg + RT / 32 - 1) / (RT / 32)), RT, 0, s>>>(
+            a, b, nseg, seg, out, rnd, word);
+    else
+        k_red_seg<FMT, MODE><<<red_blocks(nseg), RT, 0, s>>>(a, b, nseg, seg, out, rnd, word);
     return cudaGetLastError();
 }
 
