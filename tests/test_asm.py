@@ -222,3 +222,40 @@ def test_shipped_sources_against_the_reference_c_tool(tmp_path):
         assert img == out.read_bytes(), f
         q = subprocess.run([str(REF_TOOL), "-i", str(out)], capture_output=True, text=True)
         assert q.returncode == 0 and q.stdout == asm.info(img), f
+
+
+def test_c_abi_argument_checks():
+    """The C calls refuse NULL outputs and unreadable images by name, and
+    the bank call answers a size query (NULL bank, cap 0)."""
+    import ctypes
+    L = asm._L()
+    vp, sz = ctypes.c_void_p, ctypes.c_size_t
+    assert L.cftg_asm_assemble(b".format fp32\n.deposits 1\nhalt\n", 30, b"k", None, None) == 1
+    p = vp()
+    assert L.cftg_asm_disassemble(b"CFTP", 4, ctypes.byref(p)) == 1
+    assert b"header" in L.cft_last_error()
+    assert L.cftg_asm_info(b"XXXX" + bytes(28), 32, ctypes.byref(p)) == 1
+    assert b"magic" in L.cft_last_error()
+    need = sz()
+    assert L.cftg_ode_bank(b"lorenz96-rk4", 2, b"0.005", None, 0, ctypes.byref(need)) == 0
+    assert need.value == 5 * 16
+    small = ctypes.create_string_buffer(16)
+    assert L.cftg_ode_bank(b"lorenz96-rk4", 2, b"0.005", small, 16, ctypes.byref(need)) == 1
+    assert L.cftg_ode_bank(b"lorenz96-rk4", 7, b"0.005", None, 0, ctypes.byref(need)) == 1
+
+
+def test_images_the_loader_takes():
+    """Every image the assembler writes is one the library's own loader
+    takes (cftg_program_check, no device; scratch depth 2^15, the deepest
+    a tile publishes)."""
+    import ctypes
+    L = asm._L()
+    L.cftg_program_check.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_uint32]
+    n = 0
+    for rec in CORPUS["programs"]:
+        if rec["image"] is None:
+            continue
+        img = bytes.fromhex(rec["image"])
+        assert L.cftg_program_check(img, len(img), 1 << 15) == 0, L.cft_last_error()
+        n += 1
+    assert n > 200
