@@ -304,8 +304,9 @@ def sweep(h, n=1 << 24, reps=3, check_n=4096, seed=11):
     """The elementwise sweep: every format x {add, sub, mul, fma, div, sqrt}
     x rounding attribute over n device-generated operands a cell (the
     benchmark's value mix). Each cell is timed over `reps` launches with CUDA
-    events; a prefix of check_n elements is run once more with per-element
-    flag bytes and returned (operands, results, flags) for the oracle."""
+    events; the cell is run once more with per-element flag bytes and a
+    prefix of check_n elements is returned (operands, results, flags) for
+    the oracle."""
     import torch
     from . import workload as wl
     L = _lib.lib()
@@ -321,7 +322,7 @@ def sweep(h, n=1 << 24, reps=3, check_n=4096, seed=11):
         for j in range(3):
             _lib.check(L.cftg_fill_operands(fmt, ops[j].data_ptr(), n, seed * 16 + fmt * 4 + j, 64,
                                             100000, s), "cftg_fill_operands")
-        lf = torch.zeros(check_n, dtype=torch.uint8, device="cuda")
+        lf = torch.zeros(n, dtype=torch.uint8, device="cuda")
         pa, pb, pc, pd = (x.data_ptr() for x in ops)
         for name, kind, op in SWEEP_OPS:
             for rnd in range(5):
@@ -339,11 +340,13 @@ def sweep(h, n=1 << 24, reps=3, check_n=4096, seed=11):
                 ms = e0.elapsed_time(e1) / reps
                 cells.append({"fmt": ("fp32", "fp64", "fp128", "fp256")[fmt], "op": name,
                               "rnd": rnd, "ms": ms, "gelem_s": n / ms / 1e6})
-                go(check_n, lf.data_ptr())
+                # the checked prefix comes from a full-size launch (the kernel
+                # the cell timed), with per-element flag bytes
+                go(n, lf.data_ptr())
                 torch.cuda.synchronize()
                 host = [x[:check_n * W].cpu().numpy().view(np.uint32).reshape(-1, W) for x in ops]
                 checks.append(dict(fmt=fmt, kind=kind, op=op, rnd=rnd, a=host[0], b=host[1],
-                                   c=host[2], d=host[3], lf=lf.cpu().numpy().copy()))
+                                   c=host[2], d=host[3], lf=lf[:check_n].cpu().numpy().copy()))
         del ops
     return {"suite": "sweep", "elements_per_cell": n, "cells": cells, "_checks": checks}
 

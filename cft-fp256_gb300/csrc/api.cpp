@@ -694,6 +694,11 @@ static bool exec_direct(const char *who, cft_device *dev, int kind, int op, int 
         *st = poison(dev, who, e);
         return true;
     }
+    if (dev->h_word[0] & ELEM_ERR_STAGING) {
+        set_error("%s: a staged operand load did not complete in time; outputs are incomplete", who);
+        *st = CFT_ERR_INTERNAL;
+        return true;
+    }
     flags_emit(dev, dev->h_word[0] & CFT_FLAGS_ALL, flags_out);
     *st = CFT_OK;
     return true;
@@ -895,6 +900,12 @@ static cft_status exec_elem(const char *who, cft_device *dev, int kind, int op, 
     if (ready) cudaEventDestroy(ready);
     if (e0 != cudaSuccess || e1 != cudaSuccess)
         return poison(dev, who, e0 != cudaSuccess ? e0 : e1);
+    if ((dev->h_word[0] | dev->h_word[1]) & ELEM_ERR_STAGING) {
+        // a resident output holds a partial run: LOST, as after a failed run
+        if (dbuf) dbuf->state = B_LOST;
+        set_error("%s: a staged operand load did not complete in time; outputs are incomplete", who);
+        return CFT_ERR_INTERNAL;
+    }
     if (dbuf) dbuf->state = B_DIRTY;
     if (dbuf_mirror) dbuf_mirror->state = B_STALE;
     flags_emit(dev, (dev->h_word[0] | dev->h_word[1]) & CFT_FLAGS_ALL, flags_out);

@@ -34,8 +34,18 @@ struct ElemLaunch {
     uint32_t blocks_per_sm = 0;               // grid cap in blocks an SM (0: eight)
 };
 
-// Launch on `stream`; returns the launch status.
+// Bit 31 of an element launch's flag word: a bulk-staged launch
+// (elem_bulk.cu) found a stage of its shared-memory ring not filled within
+// the time limit; that launch's outputs are incomplete.
+constexpr uint32_t ELEM_ERR_STAGING = 0x80000000u;
+
+// Launch on `stream`; returns the launch status. The direct kernels
+// (elem.cu) take every launch unless CFTG_ELEM_STAGING=bulk sends large
+// arrays in device memory to the bulk-staged ones (elem_bulk.cu).
 cudaError_t launch_elem(const ElemLaunch &L, cudaStream_t stream);
+// The bulk-staged launch, when asked for and L qualifies (then *err is its
+// status and the result true); false when the direct kernels take L.
+bool launch_elem_bulk(const ElemLaunch &L, cudaStream_t stream, cudaError_t *err);
 
 // The kernels' dimensions for a given launch (used by the queue autotuner).
 int sm_count();

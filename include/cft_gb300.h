@@ -28,7 +28,11 @@ extern "C" {
  * reads it back); lane_flags, when non-NULL, receives each element's flag
  * byte. A NULL b or c reads +0. scalar_mask bit r makes operand r element
  * 0 for every i. The status word of the handle is NOT updated: the flags
- * stay on the device until the caller reads them. */
+ * stay on the device until the caller reads them. Bit 31 of the word
+ * (CFTG_FLAG_STAGING_TIMEOUT), set only by the bulk-staged kernels that
+ * CFTG_ELEM_STAGING=bulk selects, means a shared-memory stage was not
+ * filled within one second and the outputs are incomplete. */
+#define CFTG_FLAG_STAGING_TIMEOUT 0x80000000u
 CFT_API cft_status cftg_run_device(cft_device *dev, int kind, cft_op op, cft_format fmt,
                                    cft_round rnd, const void *a, const void *b, const void *c,
                                    void *d, size_t n, uint32_t scalar_mask, uint8_t *lane_flags,
