@@ -675,7 +675,10 @@ def link(h, nbytes=1 << 30, reps=3):
     """The host link's rates: copy-engine copies of pinned memory each way
     and both ways at once (torch), and this library's kernel reading and
     writing pinned host memory in place - a binary64 NEG through cft_run
-    (reads 8 bytes and writes 8 an element, almost no arithmetic)."""
+    (reads 8 bytes and writes 8 an element, almost no arithmetic); then
+    host-to-device copies split over 2 and 4 streams, and a copy beside the
+    kernel's in-place reads (each on half the bytes), to see whether the
+    link carries more than one engine or one kernel draws from it."""
     import torch
     L = _lib.lib()
     out = {}
@@ -717,4 +720,31 @@ def link(h, nbytes=1 << 30, reps=3):
     t = timed(neg)
     out["kernel_in_place_read_gbs"] = nbytes / t / 1e9
     out["kernel_in_place_write_gbs"] = nbytes / t / 1e9
+
+    # host-to-device over k streams at once (one slice each: several copy
+    # engines, if the driver spreads them)
+    extra = [torch.cuda.Stream() for _ in range(4)]
+    for k in (2, 4):
+        part = nbytes // k
+
+        def many():
+            for j in range(k):
+                with torch.cuda.stream(extra[j]):
+                    dv[j * part:(j + 1) * part].copy_(hp[j * part:(j + 1) * part], non_blocking=True)
+            for j in range(k):
+                torch.cuda.current_stream().wait_stream(extra[j])
+        out[f"h2d_{k}_streams_gbs"] = nbytes / timed(many) / 1e9
+
+    # a copy engine and the kernel's in-place reads at once, each on its own
+    # half of the bytes: their sum is what the link carries for both
+    half = nbytes // 2
+    hn = half // 8
+
+    def mixed():
+        with torch.cuda.stream(extra[0]):
+            dv[:half].copy_(hp[half:], non_blocking=True)
+        _lib.check(L.cft_run(h, 5, 1, 0, hp.data_ptr(), None, None, hq.data_ptr(), hn,
+                             ctypes.byref(fl), None), "cft_run")
+        torch.cuda.current_stream().wait_stream(extra[0])
+    out["copy_plus_kernel_read_gbs"] = 2 * half / timed(mixed) / 1e9
     return {"suite": "link", "bytes": nbytes, **out}
