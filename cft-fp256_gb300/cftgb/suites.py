@@ -48,6 +48,8 @@ def _bind(L):
     L.cftg_autotune.argtypes = [vp, vp, vp, vp, vp, ctypes.c_size_t, vp]
     L.cftg_tile_length.argtypes = [ctypes.c_int] * 3
     L.cftg_tile_length.restype = ctypes.c_uint32
+    L.cftg_queue_block_threads.argtypes = []
+    L.cftg_queue_block_threads.restype = ctypes.c_int
 
 
 def uneven(h, ncalls=10000, seed=4, max_log2=20, reps=3):
@@ -147,6 +149,7 @@ def uneven(h, ncalls=10000, seed=4, max_log2=20, reps=3):
         "tiles": int(tiles), "autotune_s": tune_s, "bit_exact_vs_plain": bool(exact),
         "tile_lengths": {f"fmt{f}": [int(L.cftg_tile_length(f, k, o)) for k, o in kinds]
                          for f in (1, 2, 3)},
+        "block_threads": int(L.cftg_queue_block_threads()),
     }
 
 

@@ -29,6 +29,10 @@ double cost(int fmt, int kind)
 // defaults that give every tile roughly the same amount of work
 uint32_t g_tile[4][7];
 bool g_tile_init = false;
+// threads a block of the work-queue launch: the autotuner's choice (a
+// block takes a whole tile, so a tile of t elements gives each thread
+// t / threads of them)
+int g_queue_threads = 256;
 
 void tile_defaults()
 {
@@ -62,7 +66,7 @@ struct cftg_batch {
     uint32_t *d_flags = nullptr;      // the caller's per-call words
     size_t ncalls = 0;
     uint32_t ntiles = 0;
-    int blocks = 0;
+    int blocks = 0, threads = 256;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
 };
@@ -143,7 +147,8 @@ extern "C" cft_status cftg_batch_create(cft_device *dev, const cftg_call *calls,
         set_error("cftg_batch_create: could not place the batch's tables on the device");
         return CFT_ERR_OUT_OF_MEMORY;
     }
-    b->blocks = sm_count() * queue_blocks_per_sm();
+    b->threads = g_queue_threads;
+    b->blocks = sm_count() * queue_blocks_per_sm(b->threads);
     *out = b;
     return CFT_OK;
 }
@@ -153,7 +158,8 @@ static cudaError_t enqueue(cftg_batch *b, cudaStream_t s)
     cudaError_t e = cudaMemsetAsync(b->d_counter, 0, sizeof(uint32_t), s);
     if (e == cudaSuccess && b->ncalls) e = cudaMemsetAsync(b->d_flags, 0, b->ncalls * sizeof(uint32_t), s);
     if (e == cudaSuccess)
-        e = launch_queue(b->d_calls, b->d_tiles, b->ntiles, b->d_counter, b->d_flags, b->blocks, s);
+        e = launch_queue(b->d_calls, b->d_tiles, b->ntiles, b->d_counter, b->d_flags, b->blocks,
+                         b->threads, s);
     return e;
 }
 
@@ -194,10 +200,12 @@ extern "C" cft_status cftg_batch_launch(cftg_batch *b, void *stream)
 
 extern "C" uint32_t cftg_batch_tiles(const cftg_batch *b) { return b ? b->ntiles : 0u; }
 
-// The autotuner: for each (format, kind) pair asked for, time the queue
-// over `n` elements of one call at each candidate tile length and keep the
-// fastest. Operands are whatever the caller's device buffers hold (sized
-// for n elements of fp256).
+// The autotuner, in two passes over the caller's device buffers (sized for
+// n elements of fp256; their contents are the operands): first, for each
+// (format, kind), the queue over one call at each candidate tile length,
+// keeping the fastest; then the launch's block shape, 128 or 256 threads
+// (the resident blocks an SM follow from occupancy), keeping the one whose
+// summed time over the same calls, at their chosen tiles, is least.
 extern "C" cft_status cftg_autotune(cft_device *dev, const void *d_a, const void *d_b,
                                     const void *d_c, void *d_d, size_t n, void *stream)
 {
@@ -211,42 +219,54 @@ extern "C" cft_status cftg_autotune(cft_device *dev, const void *d_a, const void
     uint32_t *d_fl = nullptr;
     if (cudaMalloc(&d_fl, 64 * sizeof(uint32_t)) != cudaSuccess) return CFT_ERR_OUT_OF_MEMORY;
     static const uint32_t cand[6] = {256, 1024, 4096, 16384, 65536, 262144};
+    static const int shapes[2] = {128, 256};
     const int kinds[4][2] = {{CFTG_KIND_OP, 0}, {CFTG_KIND_OP, 1}, {CFTG_KIND_DIV, 0}, {CFTG_KIND_SQRT, 0}};
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
+    // ms of three queue launches over one call of m elements (warm first)
+    auto time_call = [&](int f, const int (&kk)[2], size_t m) -> float {
+        cftg_call c;
+        memset(&c, 0, sizeof c);
+        c.kind = kk[0];
+        c.op = kk[1];
+        c.fmt = f;
+        c.a = d_a;
+        c.b = d_b;
+        c.c = d_c;
+        c.d = d_d;
+        c.n = m;
+        cftg_batch *b = nullptr;
+        if (cftg_batch_create(dev, &c, 1, d_fl, &b) != CFT_OK) return 1e30f;
+        enqueue(b, s);
+        cudaEventRecord(e0, s);
+        for (int r = 0; r < 3; r++) enqueue(b, s);
+        cudaEventRecord(e1, s);
+        cudaEventSynchronize(e1);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        cftg_batch_free(b);
+        return ms;
+    };
+    // fewer elements for the costly ones keeps the tuning quick
+    auto elems = [&](int f, int kind) {
+        size_t m = std::min(n, (size_t)(4u << 20) / (size_t)(cost(f, kind) > 20 ? 32 : 1));
+        return std::max<size_t>(m, 4096);
+    };
+    auto kind_of = [](const int (&kk)[2]) {
+        return kk[0] == CFTG_KIND_DIV ? K_DIV : kk[0] == CFTG_KIND_SQRT ? K_SQRT : elem_kind_of_op(kk[1]);
+    };
+    g_queue_threads = 256;
     for (int f = 0; f < 4; f++) {
         for (auto &kk : kinds) {
-            const int kind = kk[0] == CFTG_KIND_DIV ? K_DIV : kk[0] == CFTG_KIND_SQRT ? K_SQRT
-                                                                  : elem_kind_of_op(kk[1]);
-            // fewer elements for the costly ones keeps the tuning quick
-            size_t m = std::min(n, (size_t)(4u << 20) / (size_t)(cost(f, kind) > 20 ? 32 : 1));
-            m = std::max<size_t>(m, 4096);
+            const int kind = kind_of(kk);
+            const size_t m = elems(f, kind);
             float best = 1e30f;
             uint32_t bestt = g_tile[f][kind];
             for (uint32_t t : cand) {
                 if (t > m) break;
                 g_tile[f][kind] = t;
-                cftg_call c;
-                memset(&c, 0, sizeof c);
-                c.kind = kk[0];
-                c.op = kk[1];
-                c.fmt = f;
-                c.a = d_a;
-                c.b = d_b;
-                c.c = d_c;
-                c.d = d_d;
-                c.n = m;
-                cftg_batch *b = nullptr;
-                if (cftg_batch_create(dev, &c, 1, d_fl, &b) != CFT_OK) continue;
-                enqueue(b, s);                              // warm
-                cudaEventRecord(e0, s);
-                for (int r = 0; r < 3; r++) enqueue(b, s);
-                cudaEventRecord(e1, s);
-                cudaEventSynchronize(e1);
-                float ms = 0;
-                cudaEventElapsedTime(&ms, e0, e1);
-                cftg_batch_free(b);
+                const float ms = time_call(f, kk, m);
                 if (ms < best) {
                     best = ms;
                     bestt = t;
@@ -259,11 +279,37 @@ extern "C" cft_status cftg_autotune(cft_device *dev, const void *d_a, const void
             }
         }
     }
+    float best_sum = 1e30f;
+    int best_shape = 256;
+    for (int th : shapes) {
+        g_queue_threads = th;
+        float sum = 0.f;
+        for (int f = 0; f < 4; f++)
+            for (auto &kk : kinds) sum += time_call(f, kk, elems(f, kind_of(kk)));
+        if (sum < best_sum) {
+            best_sum = sum;
+            best_shape = th;
+        }
+    }
+    g_queue_threads = best_shape;
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     cudaFree(d_fl);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return poison(dev, "cftg_autotune", e);
+    return CFT_OK;
+}
+
+extern "C" int cftg_queue_block_threads(void) { return g_queue_threads; }
+
+extern "C" cft_status cftg_set_queue_block_threads(int threads)
+{
+    clear_error();
+    if (threads < 32 || threads > 256 || threads % 32) {
+        set_error("cftg_set_queue_block_threads: %d is not a multiple of 32 in 32..256", threads);
+        return CFT_ERR_INVALID_ARGUMENT;
+    }
+    g_queue_threads = threads;
     return CFT_OK;
 }
 

@@ -191,10 +191,10 @@ cudaError_t launch_queue_calls(const QCall *calls, const uint32_t *prefix, uint3
 }
 
 cudaError_t launch_queue(const QCall *calls, const QTile *tiles, uint32_t ntiles, uint32_t *counter,
-                         uint32_t *call_flags, int blocks, cudaStream_t s)
+                         uint32_t *call_flags, int blocks, int threads, cudaStream_t s)
 {
     if (ntiles == 0) return cudaSuccess;
-    k_queue<<<blocks, 256, 0, s>>>(calls, tiles, ntiles, counter, call_flags);
+    k_queue<<<blocks, threads, 0, s>>>(calls, tiles, ntiles, counter, call_flags);
     return cudaGetLastError();
 }
 
@@ -208,10 +208,10 @@ int queue_calls_regs()
     return fa.numRegs;
 }
 
-int queue_blocks_per_sm()
+int queue_blocks_per_sm(int threads)
 {
     int per = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_queue, 256, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_queue, threads, 0);
     return per > 0 ? per : 1;
 }
 

@@ -22,9 +22,11 @@ struct QTile {
     uint32_t call, len;
 };
 
+// k_queue over `blocks` blocks of `threads` (a multiple of 32, <= 256)
 cudaError_t launch_queue(const QCall *calls, const QTile *tiles, uint32_t ntiles, uint32_t *counter,
-                         uint32_t *call_flags, int blocks, cudaStream_t s);
-int queue_blocks_per_sm();
+                         uint32_t *call_flags, int blocks, int threads, cudaStream_t s);
+// k_queue blocks of `threads` one SM holds
+int queue_blocks_per_sm(int threads);
 // Registers a thread of the table-free work-queue kernel uses.
 int queue_calls_regs();
 

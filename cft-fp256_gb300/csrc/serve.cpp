@@ -575,7 +575,7 @@ extern "C" cft_status cftg_server_create(cft_device *dev, const cftg_server_conf
     s->dev = dev;
     s->cfg = c;
     {
-        const int per = queue_blocks_per_sm();
+        const int per = queue_blocks_per_sm(256);
         const int want = (int)std::min<uint32_t>(c.elem_blocks_per_sm ? c.elem_blocks_per_sm : 2u, (uint32_t)per);
         s->queue_blocks = sm_count() * want;
         int per_sm = 0, reserved = 0, regs_sm = 0;

@@ -93,7 +93,8 @@ template <int N> struct AddPtx;
 template <> struct AddPtx<2> {
     static __device__ __forceinline__ uint32_t add(uint32_t (&r)[2], const uint32_t (&x)[2], uint32_t cin)
     {
-        uint32_t c, scratch;
+        uint32_t c;
+        [[maybe_unused]] uint32_t scratch;   // carries cin into the chain's carry flag
         asm("add.cc.u32 %3, %6, -1;\n\taddc.cc.u32 %0, %0, %4;\n\taddc.cc.u32 %1, %1, %5;\n\taddc.u32 %2, 0, 0;"
             : "+r"(r[0]), "+r"(r[1]), "=r"(c), "=r"(scratch)
             : "r"(x[0]), "r"(x[1]), "r"(cin));
@@ -103,7 +104,8 @@ template <> struct AddPtx<2> {
 template <> struct AddPtx<4> {
     static __device__ __forceinline__ uint32_t add(uint32_t (&r)[4], const uint32_t (&x)[4], uint32_t cin)
     {
-        uint32_t c, scratch;
+        uint32_t c;
+        [[maybe_unused]] uint32_t scratch;   // carries cin into the chain's carry flag
         asm("add.cc.u32 %5, %10, -1;\n\taddc.cc.u32 %0, %0, %6;\n\taddc.cc.u32 %1, %1, %7;\n\taddc.cc.u32 %2, %2, %8;\n\taddc.cc.u32 %3, %3, %9;\n\taddc.u32 %4, 0, 0;"
             : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "=r"(c), "=r"(scratch)
             : "r"(x[0]), "r"(x[1]), "r"(x[2]), "r"(x[3]), "r"(cin));
@@ -113,7 +115,8 @@ template <> struct AddPtx<4> {
 template <> struct AddPtx<8> {
     static __device__ __forceinline__ uint32_t add(uint32_t (&r)[8], const uint32_t (&x)[8], uint32_t cin)
     {
-        uint32_t c, scratch;
+        uint32_t c;
+        [[maybe_unused]] uint32_t scratch;   // carries cin into the chain's carry flag
         asm("add.cc.u32 %9, %18, -1;\n\taddc.cc.u32 %0, %0, %10;\n\taddc.cc.u32 %1, %1, %11;\n\taddc.cc.u32 %2, %2, %12;\n\taddc.cc.u32 %3, %3, %13;\n\taddc.cc.u32 %4, %4, %14;\n\taddc.cc.u32 %5, %5, %15;\n\taddc.cc.u32 %6, %6, %16;\n\taddc.cc.u32 %7, %7, %17;\n\taddc.u32 %8, 0, 0;"
             : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]), "=r"(c), "=r"(scratch)
             : "r"(x[0]), "r"(x[1]), "r"(x[2]), "r"(x[3]), "r"(x[4]), "r"(x[5]), "r"(x[6]), "r"(x[7]), "r"(cin));
@@ -123,7 +126,8 @@ template <> struct AddPtx<8> {
 template <> struct AddPtx<16> {
     static __device__ __forceinline__ uint32_t add(uint32_t (&r)[16], const uint32_t (&x)[16], uint32_t cin)
     {
-        uint32_t c, scratch;
+        uint32_t c;
+        [[maybe_unused]] uint32_t scratch;   // carries cin into the chain's carry flag
         asm("add.cc.u32 %17, %34, -1;\n\taddc.cc.u32 %0, %0, %18;\n\taddc.cc.u32 %1, %1, %19;\n\taddc.cc.u32 %2, %2, %20;\n\taddc.cc.u32 %3, %3, %21;\n\taddc.cc.u32 %4, %4, %22;\n\taddc.cc.u32 %5, %5, %23;\n\taddc.cc.u32 %6, %6, %24;\n\taddc.cc.u32 %7, %7, %25;\n\taddc.cc.u32 %8, %8, %26;\n\taddc.cc.u32 %9, %9, %27;\n\taddc.cc.u32 %10, %10, %28;\n\taddc.cc.u32 %11, %11, %29;\n\taddc.cc.u32 %12, %12, %30;\n\taddc.cc.u32 %13, %13, %31;\n\taddc.cc.u32 %14, %14, %32;\n\taddc.cc.u32 %15, %15, %33;\n\taddc.u32 %16, 0, 0;"
             : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]), "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]), "+r"(r[14]), "+r"(r[15]), "=r"(c), "=r"(scratch)
             : "r"(x[0]), "r"(x[1]), "r"(x[2]), "r"(x[3]), "r"(x[4]), "r"(x[5]), "r"(x[6]), "r"(x[7]), "r"(x[8]), "r"(x[9]), "r"(x[10]), "r"(x[11]), "r"(x[12]), "r"(x[13]), "r"(x[14]), "r"(x[15]), "r"(cin));

@@ -81,13 +81,21 @@ CFT_API cft_status cftg_batch_capture(cftg_batch *b, void *stream);
 CFT_API void cftg_batch_free(cftg_batch *b);
 CFT_API uint32_t cftg_batch_tiles(const cftg_batch *b);
 
-/* The tile-length autotuner: times the work queue at candidate tile
- * lengths for each format and for FMA, ADD, DIV and SQRT over n elements
- * of the caller's device buffers (each sized for n binary256 elements),
- * and keeps the fastest for every later batch in the process. */
+/* The work queue's autotuner: times the queue at candidate tile lengths
+ * (elements a tile: 256 .. 262,144) for each format and for FMA, ADD, DIV
+ * and SQRT over n elements of the caller's device buffers (each sized for
+ * n binary256 elements), then the launch's block shape (128 or 256
+ * threads), and keeps the fastest of each for every batch created later in
+ * the process. */
 CFT_API cft_status cftg_autotune(cft_device *dev, const void *d_a, const void *d_b,
                                  const void *d_c, void *d_d, size_t n, void *stream);
+/* Elements a tile the batched form cuts a call of (fmt, kind, op) into. */
 CFT_API uint32_t cftg_tile_length(int fmt, int kind, int op);
+/* Threads a block of the batched form's work-queue launch (256 until the
+ * autotuner has run), and the setter for callers that choose it
+ * themselves (a multiple of 32 in 32..256; batches created later use it). */
+CFT_API int cftg_queue_block_threads(void);
+CFT_API cft_status cftg_set_queue_block_threads(int threads);
 
 /* ---- trajectories: the batched sequencer ------------------------------
  *

@@ -111,3 +111,19 @@ def test_open_without_a_gpu_fails_loudly():
     assert st == 3                                  # CFT_ERR_NO_DEVICE, no CPU fallback
     assert b"no CPU fallback" in L.cft_last_error()
     assert L.cft_open(b"xclbin/tile.xclbin", 0, ctypes.byref(h)) == 3
+
+
+def test_queue_block_shape_setter_checks_its_argument():
+    """the batched form's block shape: multiples of 32 in 32..256 only"""
+    L = _lib.lib()
+    L.cftg_set_queue_block_threads.argtypes = [ctypes.c_int]
+    L.cftg_queue_block_threads.restype = ctypes.c_int
+    before = L.cftg_queue_block_threads()
+    try:
+        for bad in (0, 16, 100, 288, 512, -32):
+            assert L.cftg_set_queue_block_threads(bad) == 1, bad
+            assert L.cftg_queue_block_threads() == before
+        assert L.cftg_set_queue_block_threads(128) == 0
+        assert L.cftg_queue_block_threads() == 128
+    finally:
+        L.cftg_set_queue_block_threads(before)

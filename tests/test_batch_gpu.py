@@ -20,9 +20,21 @@ class Call(ctypes.Structure):
                 ("scalar_mask", ctypes.c_uint32)]
 
 
-def test_queue_matches_plain_launches(gpu):
+@pytest.mark.parametrize("threads", [256, 128])
+def test_queue_matches_plain_launches(gpu, threads):
+    """at both block shapes the autotuner chooses between"""
     import torch
     L = cftgb.lib()
+    before = L.cftg_queue_block_threads()
+    cftgb._lib.check(L.cftg_set_queue_block_threads(threads), "cftg_set_queue_block_threads")
+    try:
+        _queue_matches_plain(gpu, L)
+    finally:
+        cftgb._lib.check(L.cftg_set_queue_block_threads(before), "cftg_set_queue_block_threads")
+
+
+def _queue_matches_plain(gpu, L):
+    import torch
     vp = ctypes.c_void_p
     L.cftg_batch_create.argtypes = [vp, ctypes.POINTER(Call), ctypes.c_size_t, vp, ctypes.POINTER(vp)]
     L.cftg_batch_launch.argtypes = [vp, vp]
