@@ -97,6 +97,80 @@ SFD void shr_jam(uint32_t (&x)[N], int s)
     x[0] |= (st != 0u) ? 1u : 0u;
 }
 
+// 32-bit multiply-adds as the IMAD pipe runs them (kept as PTX so that a
+// multiplier known to be 0 or 1 is not turned back into a select).
+SFD uint32_t imul(uint32_t a, uint32_t b)
+{
+    uint32_t r;
+    asm("mul.lo.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(b));
+    return r;
+}
+SFD uint32_t imad(uint32_t a, uint32_t b, uint32_t c)
+{
+    uint32_t r;
+    asm("mad.lo.u32 %0, %1, %2, %3;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
+    return r;
+}
+
+// shr_jam with the select network's word moves as multiply-adds by 0 and 1
+// (x[i] = x[i+b] * take + x[i] * !take): the same bits, computed on the
+// IMAD pipe instead of the integer ALU pipe, which the kernels around it
+// keep busier.
+template <int N>
+SFD void shr_jam_imad(uint32_t (&x)[N], int s)
+{
+    const int sc = s <= 0 ? 0 : (s >= 32 * N ? 32 * N : s);
+    const int ws = sc >> 5, bs = sc & 31;                 // ws may be N
+    uint32_t st = 0u;
+    const int need = warp_stages(ws);
+#pragma unroll
+    for (int b = 16; b >= 1; b >>= 1) {
+        if (b <= N && (need & b)) {
+            const uint32_t t = (uint32_t)(ws & b) / (uint32_t)b;   // 0 or 1
+            const uint32_t nt = t ^ 1u;
+            uint32_t out = 0u;
+#pragma unroll
+            for (int i = 0; i < b; i++) out |= x[i];
+            st |= imul(out, t);
+#pragma unroll
+            for (int i = 0; i < N; i++)
+                x[i] = (i + b < N) ? imad(x[i + b], t, imul(x[i], nt)) : imul(x[i], nt);
+        }
+    }
+    st |= x[0] & ((1u << bs) - 1u);
+#pragma unroll
+    for (int i = 0; i < N - 1; i++) x[i] = __funnelshift_r(x[i], x[i + 1], bs);
+    x[N - 1] >>= bs;
+    x[0] |= (st != 0u) ? 1u : 0u;
+}
+
+// shl with the word moves and the bit shift as multiply-adds: x[i] << bs
+// is the low word of x[i] * 2^bs and x[i-1] >> (32 - bs) its high word.
+template <int N>
+SFD void shl_imad(uint32_t (&x)[N], int s)
+{
+    const int ws = s >> 5, bs = s & 31;
+    const int need = warp_stages(ws);
+#pragma unroll
+    for (int b = 16; b >= 1; b >>= 1) {
+        if (b < N && (need & b)) {
+            const uint32_t t = (uint32_t)(ws & b) / (uint32_t)b;
+            const uint32_t nt = t ^ 1u;
+#pragma unroll
+            for (int i = N - 1; i >= 0; i--)
+                x[i] = (i - b >= 0) ? imad(x[i - b], t, imul(x[i], nt)) : imul(x[i], nt);
+        }
+    }
+    const uint32_t m = 1u << bs;
+#pragma unroll
+    for (int i = N - 1; i >= 1; i--) {
+        uint32_t r;
+        asm("mad.hi.u32 %0, %1, %2, %3;" : "=r"(r) : "r"(x[i - 1]), "r"(m), "r"(imul(x[i], m)));
+        x[i] = r;
+    }
+    x[0] = imul(x[0], m);
+}
+
 // x >>= s for 0 <= s < 32N, logical (no jam).
 template <int N>
 SFD void shr(uint32_t (&x)[N], int s)

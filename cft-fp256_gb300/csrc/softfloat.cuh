@@ -215,7 +215,10 @@ SFD void round_pack(int sign, uint32_t (&m)[N], int e, int rnd, uint32_t (&out)[
     else if (__all_sync(am, m[N - 1] == 0u && m[N - 2] != 0u)) L = 32 * (N - 1) - __clz(m[N - 2]);
     else L = sfw::bitlen(m);
     const int e_norm = e + L - 1;                 // exponent of the leading bit
-    sfw::shl(m, 32 * N - L);                      // leading bit to the top
+    // leading bit to the top; narrow windows shift on the IMAD pipe, wide
+    // ones (whose products already load it) on the integer ALU
+    if constexpr (N <= 5) sfw::shl_imad(m, 32 * N - L);
+    else sfw::shl(m, 32 * N - L);
 
     uint32_t kept[W];
     bool guard, sticky;
@@ -344,21 +347,32 @@ SFD void fma_general(const Unp<FMT> &ua, const Unp<FMT> &ub, const Unp<FMT> &uc,
         const int delta = czero ? -(1 << 28) : uc.ve - (ew + 64 * W - 2);
         const bool pbig = delta <= 0;
         uint32_t X[N], Y[N];
+        // the selections as multiply-adds by 0 and 1 (IMAD pipe)
+        {
+            const uint32_t pb = pbig ? 1u : 0u, npb = pb ^ 1u;
 #pragma unroll
-        for (int i = 0; i < N; i++) {
-            X[i] = pbig ? C[i] : P[i];
-            Y[i] = pbig ? P[i] : C[i];
+            for (int i = 0; i < N; i++) {
+                if (i < W) {                          // C's low words are zero
+                    X[i] = sfw::imul(P[i], npb);
+                    Y[i] = sfw::imul(P[i], pb);
+                } else {
+                    X[i] = sfw::imad(C[i], pb, sfw::imul(P[i], npb));
+                    Y[i] = sfw::imad(P[i], pb, sfw::imul(C[i], npb));
+                }
+            }
         }
-        sfw::shr_jam(X, pbig ? -delta : delta);
+        sfw::shr_jam_imad(X, pbig ? -delta : delta);
         if (!pbig) ew += delta;
         const int s_big = pbig ? sp : sc, s_small = pbig ? sc : sp;
         // Y + X, or Y - X in two's complement, then the magnitude.
         const bool sub = sp != sc;
         const uint32_t mk = sub ? 0xFFFFFFFFu : 0u;
+        // X ^ mk as X * m1 + mk (~X is -X - 1 modulo 2^32), on the IMAD pipe
+        const uint32_t m1 = sub ? 0xFFFFFFFFu : 1u;
 #pragma unroll
         for (int i = 0; i < N; i++) {
             P[i] = Y[i];
-            X[i] ^= mk;
+            X[i] = sfw::imad(X[i], m1, mk);
         }
         const uint32_t cy = sfw::AddPtx<N>::add(P, X, sub ? 1u : 0u);
         const bool neg = sub && !cy;               // Y < X: the result is X - Y
