@@ -141,15 +141,18 @@ __global__ void __launch_bounds__(256) k_elem_bulk(const ElemLaunch L, const uns
     if (lane == 0 && acc) atomicOr(L.flags, acc);
 }
 
+// p is 16-byte aligned memory of the current device (not host memory, not
+// managed memory, not another GPU's).
 bool in_hbm(const void *p)
 {
     if (reinterpret_cast<uintptr_t>(p) & 15u) return false;
     cudaPointerAttributes at;
-    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    int dev = -1;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess || cudaGetDevice(&dev) != cudaSuccess) {
         cudaGetLastError();
         return false;
     }
-    return at.type == cudaMemoryTypeDevice;
+    return at.type == cudaMemoryTypeDevice && at.device == dev;
 }
 
 // The ring's shared memory asks for the opt-in ceiling and the largest
