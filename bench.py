@@ -47,9 +47,10 @@ METRIC = "fp256/fp128 FMA Gelem/s bit-exact (plain vs batched); mixed-load p50/p
 # copy engines' host-to-device rate and a streaming kernel's, which agree;
 # bench.py --suite link measures it)
 LINK_READ_GBS = 211.0
-# DRAM bytes (read + write) an element of the FMA kernel, from the ncu
-# capture summarised in profiles/k_elem_fma256_n4M.md (402.7 + 112.7 MB / 4,194,304)
-TRAFFIC_B_PER_ELEM = {3: 515.4e6 / 4194304}
+# DRAM bytes (read + write) an element of the FMA kernel: dram__bytes_read.sum
+# + dram__bytes_write.sum of one ncu-captured launch over 4,194,304 elements
+# of the same operand mix (402.7 + 112.3 MB)
+TRAFFIC_B_PER_ELEM = {3: 515.05e6 / 4194304}
 N_DEFAULT = 1 << 24
 
 
