@@ -12,6 +12,17 @@ def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (a GB300); parity tests proper")
 
 
+def pytest_sessionstart(session):
+    """A fresh checkout has no library yet: build it (nvcc cross-compiles
+    without a GPU) before any test loads it."""
+    import os
+    if os.environ.get("CFTG_LIB"):
+        return
+    from cftgb import build
+    if not build.LIB.exists():
+        build.build_lib()
+
+
 @pytest.fixture(scope="session")
 def oracle():
     import oracle_lib
