@@ -95,3 +95,69 @@ def test_oracle_planted_mistake_is_caught(oracle):
                           g["c"][i:i + 1])
     d[0, 0] ^= 1
     assert not np.array_equal(d[0], g["d"][i])
+
+
+def _raw_and_boundary(fmt, n, seed):
+    """Operands drawn over the whole encoding space: uniform random words
+    (every exponent, so far-apart alignments, NaN payloads and subnormals),
+    then the same words with exponents moved next to the overflow and the
+    underflow thresholds (products and sums that overflow, results that land
+    in the subnormal range or round across its edges)."""
+    g = wl.geometry(fmt)
+    W, es, expw = g["W"], g["es"], g["expw"]
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(3):
+        x = rng.integers(0, 1 << 32, size=(n, W), dtype=np.uint64).astype(np.uint32)
+        third = n // 3
+        emax = (1 << expw) - 2
+        near = np.concatenate([rng.integers(max(1, emax - 3 * g["prec"]), emax + 1, size=third),
+                               rng.integers(1, 3 * g["prec"], size=third)]).astype(np.uint32)
+        top = x[n - 2 * third:, W - 1]
+        top &= np.uint32(~(((1 << expw) - 1) << es) & 0xFFFFFFFF)
+        top |= near << np.uint32(es)
+        x[n - 2 * third:, W - 1] = top
+        out.append(x)
+    return out
+
+
+@pytest.mark.parametrize("fmt", [0, 1, 2, 3])
+def test_oracle_matches_reference_on_raw_encodings(oracle, fmt):
+    """FMA/ADD/SUB/MUL, division and square root under every attribute over
+    raw and boundary encodings: the same values and, element by element on a
+    slice, the same flags as the reference library."""
+    L, dev = _ref()
+    n = 1500
+    a, b, c = _raw_and_boundary(fmt, n, 31 + fmt)
+    for kind, op in ((0, 0), (0, 1), (0, 2), (0, 3), (1, 0), (2, 0)):
+        for rnd in range(5):
+            d, lf, acc = oracle.run(kind, fmt, op, rnd, a, b, c)
+            ref = np.zeros_like(d)
+            fl = ctypes.c_uint32()
+            if kind == 0:
+                st = L.cft_run(dev, op, fmt, rnd, a.ctypes.data, b.ctypes.data, c.ctypes.data,
+                               ref.ctypes.data, ctypes.c_size_t(n), ctypes.byref(fl), None)
+            elif kind == 1:
+                st = L.cft_div(dev, fmt, rnd, a.ctypes.data, b.ctypes.data, ref.ctypes.data,
+                               ctypes.c_size_t(n), ctypes.byref(fl), None)
+            else:
+                st = L.cft_sqrt(dev, fmt, rnd, a.ctypes.data, ref.ctypes.data,
+                                ctypes.c_size_t(n), ctypes.byref(fl), None)
+            assert st == 0
+            bad = np.nonzero((d != ref).any(1))[0]
+            assert bad.size == 0, (kind, op, rnd, bad[:5])
+            assert acc == fl.value, (kind, op, rnd)
+            for i in range(0, n, 53):
+                one = np.zeros((1, a.shape[1]), np.uint32)
+                f1 = ctypes.c_uint32()
+                if kind == 0:
+                    L.cft_run(dev, op, fmt, rnd, a[i:].ctypes.data, b[i:].ctypes.data,
+                              c[i:].ctypes.data, one.ctypes.data, ctypes.c_size_t(1),
+                              ctypes.byref(f1), None)
+                elif kind == 1:
+                    L.cft_div(dev, fmt, rnd, a[i:].ctypes.data, b[i:].ctypes.data,
+                              one.ctypes.data, ctypes.c_size_t(1), ctypes.byref(f1), None)
+                else:
+                    L.cft_sqrt(dev, fmt, rnd, a[i:].ctypes.data, one.ctypes.data,
+                               ctypes.c_size_t(1), ctypes.byref(f1), None)
+                assert lf[i] == f1.value, (kind, op, rnd, i)
