@@ -127,3 +127,60 @@ def test_schedule_parallelism():
     assert n32 * 8 < n1, (n1, n32)
     dep = next(p for p in su.cases() if su.header(su.load(p)["image"])["maxdep"] > 0)
     assert schedule(su.load(dep)["image"].copy(), 4) is None
+
+
+def _arith_sites(img):
+    hd = su.header(img)
+    esz = (4, 8, 16, 32)[hd["prec"]]
+    base = 32 + (0 if hd["flags"] & 1 else hd["n_consts"] * esz)
+    out = []
+    for i in range(hd["n_insns"]):
+        w = int.from_bytes(bytes(img[base + 8 * i:base + 8 * i + 8]), "little")
+        if not (w >> 27) & 0x1F:              # no constant flags, kx or ctrl
+            out.append(base + 8 * i)
+    return out
+
+
+@pytest.mark.parametrize("key,fmt,slots,base,count", [
+    ("l63", 3, 3, 1.0, 24), ("hh", 3, 4, None, 24), ("l96", 2, 40, 8.0, 6)],
+    ids=["l63", "hh", "l96"])
+def test_schedule_replay_on_mutated_programs(oracle, key, fmt, slots, base, count):
+    """Seeded bit flips in the opcode, register and rounding fields of the
+    ODE programs' arithmetic instructions give dependence patterns the
+    shipped programs do not have (reads before writes, overwritten operands,
+    reused registers); for every mutant the sequencer accepts and the
+    scheduler takes, the replay at G = 1, 4 and 32 equals the sequencer."""
+    oracle.L.sfp_compute.argtypes = [ctypes.c_int] * 3 + [ctypes.c_void_p] * 4 + [
+        ctypes.POINTER(ctypes.c_uint32)]
+    z = np.load(su.GOLD / "odes.npz")
+    img0, bank = z[key + "_image"].copy(), z[key + "_bank"].copy()
+    W = wl.words(fmt)
+    if base is None:
+        init = suites.hh_init(1, 9)
+    else:
+        init, _ = suites.ode_lanes(key, fmt, 1, slots, base, (100, 100), 100, 3)
+    sites = _arith_sites(img0)
+    rng = np.random.default_rng(7 + fmt)
+    compared = 0
+    for _ in range(count):
+        img = img0.copy()
+        for _ in range(int(rng.integers(1, 4))):
+            off = sites[int(rng.integers(0, len(sites)))]
+            bit = int(rng.choice([*range(0, 24), 24, 25, 26]))
+            img[off + bit // 8] ^= np.uint8(1 << (bit % 8))
+        out = np.zeros_like(init)
+        A = oracle_lib.SeqArgs()
+        a = np.zeros((1, W), np.uint32)
+        A.a, A.n, A.bank = a.ctypes.data, 1, bank.ctypes.data
+        A.scratch_in, A.scratch_out, A.depth = init.ctypes.data, out.ctypes.data, 256
+        if oracle.L.sfp_seq_run(img.ctypes.data, img.size, ctypes.byref(A)) != 0:
+            continue
+        for G in (1, 4, 32):
+            sched = schedule(img, G)
+            if sched is None:
+                break
+            got, gflags = replay(oracle, sched, fmt, bank, init, 256, W)
+            assert np.array_equal(got[:slots], out), (key, G)
+            assert gflags == A.flags_out, (key, G)
+            compared += 1
+    assert compared >= count, (key, compared)
