@@ -112,3 +112,39 @@ def test_segmented_reductions_match_reference(oracle):
                     assert oracle.L.sfp_reduce_seg(fmt, op, 1, A.ctypes.data, B.ctypes.data,
                                                    d_or.ctypes.data, n, seg, ctypes.byref(f_or)) == 0
                     assert np.array_equal(d_ref, d_or) and f_ref.value == f_or.value, (fmt, op, seg)
+
+
+def _wide(fmt, n, seed):
+    """Raw random encodings (every exponent: NaN payloads, subnormals, huge
+    alignment gaps) and values next to the overflow threshold (sums that
+    overflow), half and half."""
+    g = wl.geometry(fmt)
+    W, es, expw = g["W"], g["es"], g["expw"]
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(2):
+        x = rng.integers(0, 1 << 32, size=(n, W), dtype=np.uint64).astype(np.uint32)
+        half = n // 2
+        emax = (1 << expw) - 2
+        top = x[half:, W - 1] & np.uint32(~(((1 << expw) - 1) << es) & 0xFFFFFFFF)
+        near = rng.integers(emax - 4, emax + 1, size=n - half).astype(np.uint32)
+        x[half:, W - 1] = top | (near << np.uint32(es))
+        out.append(x)
+    return out
+
+
+@pytest.mark.parametrize("fmt", [0, 1, 2, 3])
+def test_reductions_over_wide_encodings_match_reference(oracle, fmt):
+    L, dev = _ref()
+    _bind(oracle)
+    for op in OPS:
+        for n in (2, 7, 64, 513):
+            a, b = _wide(fmt, n, 3000 * fmt + n)
+            for rnd in range(5):
+                d_ref, f_ref, d_or, f_or = run_both(L, dev, oracle, fmt, op, rnd, a, b, n)
+                assert np.array_equal(d_ref, d_or) and f_ref == f_or, (op, n, rnd)
+            # the tail alone: every value near the overflow threshold
+            t = n - n // 2
+            a2, b2 = a[n // 2:].copy(), b[n // 2:].copy()
+            d_ref, f_ref, d_or, f_or = run_both(L, dev, oracle, fmt, op, 0, a2, b2, t)
+            assert np.array_equal(d_ref, d_or) and f_ref == f_or, (op, t, "near max")
