@@ -165,7 +165,7 @@ def ode_programs(scale=1.0, steps_scale=1.0):
     step sizes), seeded initial states and uneven run counts. `scale`
     scales the lane counts and `steps_scale` the step range (both 1 for
     the configuration; smaller for profiler captures)."""
-    from cftgb import suites
+    import bench_suites as suites
     z = np.load(ROOT / "tests" / "golden" / "odes.npz")
     progs = []
     for i, (name, key, fmt, slots, base, rng, spr, lanes, every) in enumerate(ODE_PROGRAMS):
@@ -187,7 +187,8 @@ def traj_oracle_check(progs, res, per_prog=8):
     sys.path.insert(0, str(ROOT / "tests"))
     import hashlib
     import oracle_lib
-    from cftgb import suites, workload as wl
+    import bench_suites as suites
+    from cftgb import workload as wl
     o = oracle_lib.Oracle()
     jobs = []
     for P, R in zip(progs, res["programs"]):
@@ -406,7 +407,7 @@ def main():
     if args.suite:
         import torch
         import cftgb
-        from cftgb import suites
+        import bench_suites as suites
         torch.cuda.set_device(0)
         h = cftgb.open_device("cuda:0")
         if args.suite == "trajectories":

@@ -25,7 +25,7 @@ import time
 
 import numpy as np
 
-from . import _lib
+from cftgb import _lib
 
 
 class Call(ctypes.Structure):
@@ -174,7 +174,7 @@ def ode_lanes(kind, fmt, lanes, slots, base, steps_range, steps_per_run, seed):
     """Seeded initial blocks (lane-major, `slots` elements a lane: base +
     N(0, 1e-3) each, rounded to double then widened exactly) and run counts
     (steps log-uniform in steps_range, rounded to whole runs)."""
-    from . import workload as wl
+    from cftgb import workload as wl
     W = wl.words(fmt)
     rng = np.random.default_rng(seed)
     vals = base + rng.normal(0.0, 1e-3, size=(lanes, slots))
@@ -209,7 +209,7 @@ def trajectories(h, progs, reps=2, separate=False):
     times from the same initial states (the first launch is the warm one),
     and returns timings plus each program's final states and hashes."""
     import torch
-    from . import workload as wl
+    from cftgb import workload as wl
     L = _lib.lib()
     _bind_traj(L)
     vp = ctypes.c_void_p
@@ -311,7 +311,7 @@ def sweep(h, n=1 << 24, reps=3, check_n=4096, seed=11):
     prefix of check_n elements is returned (operands, results, flags) for
     the oracle."""
     import torch
-    from . import workload as wl
+    from cftgb import workload as wl
     L = _lib.lib()
     _bind(L)
     stream = torch.cuda.current_stream()
@@ -358,7 +358,7 @@ def hh_init(lanes, seed):
     """Henon-Heiles initial blocks (x, y, px, py) at energy 1/8, lane-major
     binary256: x = 0, y and py drawn, px from the energy in double, each
     value widened exactly."""
-    from . import workload as wl
+    from cftgb import workload as wl
     rng = np.random.default_rng(seed)
     out = np.zeros((lanes * 4, 8), np.uint32)
     for i in range(lanes):
@@ -391,8 +391,8 @@ def serving(h, hh_image, hh_bank, rate=20000.0, seconds=60.0, seed=5, budget=40 
     alone: pinning memory while requests arrive would stall the submitting
     thread and charge the stall to the requests behind it."""
     import torch
-    from . import serving as sv
-    from . import workload as wl
+    from cftgb import serving as sv
+    from cftgb import workload as wl
     L = _lib.lib()
     _bind(L)
     sv._bind(L)
@@ -600,7 +600,7 @@ def reduce(h, n=1 << 24, reps=3, check_n=65536, seed=17, seg_sizes=(1024, 65536)
     segments of them) are reduced again and returned with their operands
     for the oracle."""
     import torch
-    from . import workload as wl
+    from cftgb import workload as wl
     L = _lib.lib()
     _bind(L)
     vp = ctypes.c_void_p

@@ -23,7 +23,10 @@
 // address. Its device address is looked up once per device with
 // cudaGetSymbolAddress, with that device current, on the first call made
 // on that device; that first call should therefore come before any stream
-// capture.
+// capture. The address is kept for the life of the process: a caller that
+// resets a device (cudaDeviceReset) or otherwise destroys its primary
+// context reloads the library's module there, at another address, so such
+// a caller must not use this entry point on that device afterwards.
 #include <mutex>
 
 #include "../../include/cft_gb300.h"
@@ -75,6 +78,11 @@ extern "C" cft_status cftg_program_run_noalloc(cft_program *prog, const void *d_
         return CFT_ERR_INVALID_ARGUMENT;
     }
     SeqProgram P = *pp;
+    if (dev->poisoned) {
+        set_error("cftg_program_run_noalloc: this handle failed earlier; close it and open it "
+                  "again");
+        return CFT_ERR_INTERNAL;
+    }
     if (n == 0) {
         flags_emit(dev, 0, flags_out);
         return CFT_OK;

@@ -74,4 +74,31 @@ extern "C" cft_status cft_max_mag(cft_device *, cft_format, const void *, const 
 extern "C" cft_status cft_minnum_mag(cft_device *, cft_format, const void *, const void *, void *, size_t, uint32_t *) { clear_error(); return refuse("cft_minnum_mag"); }
 extern "C" cft_status cft_maxnum_mag(cft_device *, cft_format, const void *, const void *, void *, size_t, uint32_t *) { clear_error(); return refuse("cft_maxnum_mag"); }
 
-
+extern "C" cft_status cft_rint(cft_device *, cft_format, cft_round, int, const void *, void *, size_t, uint32_t *, uint32_t *) { clear_error(); return refuse("cft_rint"); }
+extern "C" cft_status cft_scaleb(cft_device *, cft_format, cft_round, const void *, int64_t, void *, size_t, uint32_t *, uint32_t *) { clear_error(); return refuse("cft_scaleb"); }
+extern "C" cft_status cft_cmp_sig(cft_device *, cft_op, cft_format, const void *, const void *, void *, size_t, uint32_t *, uint32_t *) { clear_error(); return refuse("cft_cmp_sig"); }
+extern "C" cft_status cft_convert(cft_device *, cft_format, cft_format, cft_round, const void *, void *, size_t, uint32_t *) { clear_error(); return refuse("cft_convert"); }
+extern "C" cft_status cft_cvt_from_i32(cft_device *, cft_format, cft_round, const int32_t *, void *, size_t, uint32_t *) { clear_error(); return refuse("cft_cvt_from_i32"); }
+extern "C" cft_status cft_cvt_from_u32(cft_device *, cft_format, cft_round, const uint32_t *, void *, size_t, uint32_t *) { clear_error(); return refuse("cft_cvt_from_u32"); }
+extern "C" cft_status cft_cvt_from_i64(cft_device *, cft_format, cft_round, const int64_t *, void *, size_t, uint32_t *) { clear_error(); return refuse("cft_cvt_from_i64"); }
+extern "C" cft_status cft_cvt_from_u64(cft_device *, cft_format, cft_round, const uint64_t *, void *, size_t, uint32_t *) { clear_error(); return refuse("cft_cvt_from_u64"); }
+extern "C" cft_status cft_cvt_to_i32(cft_device *, cft_format, cft_round, int, const void *, int32_t *, size_t, uint32_t *) { clear_error(); return refuse("cft_cvt_to_i32"); }
+extern "C" cft_status cft_cvt_to_u32(cft_device *, cft_format, cft_round, int, const void *, uint32_t *, size_t, uint32_t *) { clear_error(); return refuse("cft_cvt_to_u32"); }
+extern "C" cft_status cft_cvt_to_i64(cft_device *, cft_format, cft_round, int, const void *, int64_t *, size_t, uint32_t *) { clear_error(); return refuse("cft_cvt_to_i64"); }
+extern "C" cft_status cft_cvt_to_u64(cft_device *, cft_format, cft_round, int, const void *, uint64_t *, size_t, uint32_t *) { clear_error(); return refuse("cft_cvt_to_u64"); }
+extern "C" cft_status cft_logb(cft_device *, cft_format, const void *, void *, size_t, uint32_t *) { clear_error(); return refuse("cft_logb"); }
+extern "C" cft_status cft_next_up(cft_device *, cft_format, const void *, void *, size_t, uint32_t *) { clear_error(); return refuse("cft_next_up"); }
+extern "C" cft_status cft_next_down(cft_device *, cft_format, const void *, void *, size_t, uint32_t *) { clear_error(); return refuse("cft_next_down"); }
+extern "C" cft_status cft_class(cft_device *, cft_format, const void *, uint8_t *, size_t) { clear_error(); return refuse("cft_class"); }
+extern "C" cft_status cft_total_order(cft_device *, cft_format, const void *, const void *, void *, size_t) { clear_error(); return refuse("cft_total_order"); }
+extern "C" cft_status cft_total_order_mag(cft_device *, cft_format, const void *, const void *, void *, size_t) { clear_error(); return refuse("cft_total_order_mag"); }
+extern "C" cft_status cft_rem(cft_device *, cft_format, const void *, const void *, void *, size_t, uint32_t *) { clear_error(); return refuse("cft_rem"); }
+extern "C" cft_status cft_conformance(cft_device *, const char *, char *report, size_t report_size, uint64_t *cases_checked)
+{
+    clear_error();
+    if (cases_checked)
+        *cases_checked = 0;
+    if (report && report_size)
+        report[0] = 0;
+    return refuse("cft_conformance");
+}

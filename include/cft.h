@@ -335,4 +335,9 @@ CFT_API int cft_is754version2019(void);
 }
 #endif
 
+/* the reference's entry points outside this backend's path, each a refusal
+ * by name: with them this header declares every function the reference's
+ * cft.h exports, so a C caller of the reference compiles and links here */
+#include "cft_unsupported.h"
+
 #endif /* CFT_H */

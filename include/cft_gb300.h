@@ -201,8 +201,13 @@ CFT_API size_t cftg_reduce_partial_bytes(int fmt, size_t n);
  * CFT_ERR_INVALID_ARGUMENT and a sentence saying by how much. Every call
  * shares the array: calls whose work overlaps on the GPU race, so issue
  * them one after another (each returns after `stream` has finished its
- * run). The first call on a device looks up the array's device address;
- * make that first call before any stream capture. */
+ * run), never from two threads or on two streams at once. The first call
+ * on a device looks up the array's device address; make that first call
+ * before any stream capture. That address is kept until the process
+ * exits, so after a cudaDeviceReset (or anything else that destroys the
+ * device's primary context) this entry point must not be used on that
+ * device again. A handle that failed earlier is refused, as the other
+ * entry points refuse it. */
 CFT_API cft_status cftg_program_run_noalloc(cft_program *prog, const void *d_a, const void *d_b,
                                             const void *d_c, const void *d_bank,
                                             const void *d_scratch_in, void *d_scratch_out,

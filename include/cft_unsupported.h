@@ -82,6 +82,37 @@ CFT_API cft_status cft_max_mag(cft_device *dev, cft_format fmt, const void *a, c
 CFT_API cft_status cft_minnum_mag(cft_device *dev, cft_format fmt, const void *a, const void *b, void *d, size_t n, uint32_t *flags_out);
 CFT_API cft_status cft_maxnum_mag(cft_device *dev, cft_format fmt, const void *a, const void *b, void *d, size_t n, uint32_t *flags_out);
 
+/* clause-5 operations off the hot path: roundToIntegral, scaleB, signaling
+ * comparisons, conversions between formats and to and from integers, logB,
+ * nextUp/nextDown, class, totalOrder, remainder (cft.h:1438-1569) */
+typedef enum cft_class_value {
+    CFT_CLASS_NEG_INF = 0, CFT_CLASS_NEG_NORM = 1, CFT_CLASS_NEG_SUB = 2, CFT_CLASS_NEG_ZERO = 3,
+    CFT_CLASS_POS_ZERO = 4, CFT_CLASS_POS_SUB = 5, CFT_CLASS_POS_NORM = 6, CFT_CLASS_POS_INF = 7,
+    CFT_CLASS_SNAN = 8, CFT_CLASS_QNAN = 9
+} cft_class_value;
+CFT_API cft_status cft_rint(cft_device *dev, cft_format fmt, cft_round rnd, int exact, const void *a, void *d, size_t n, uint32_t *flags_out, uint32_t *bus_out);
+CFT_API cft_status cft_scaleb(cft_device *dev, cft_format fmt, cft_round rnd, const void *a, int64_t nexp, void *d, size_t n, uint32_t *flags_out, uint32_t *bus_out);
+CFT_API cft_status cft_cmp_sig(cft_device *dev, cft_op cmp, cft_format fmt, const void *a, const void *b, void *d, size_t n, uint32_t *flags_out, uint32_t *bus_out);
+CFT_API cft_status cft_convert(cft_device *dev, cft_format sfmt, cft_format dfmt, cft_round rnd, const void *a, void *d, size_t n, uint32_t *flags_out);
+CFT_API cft_status cft_cvt_from_i32(cft_device *dev, cft_format fmt, cft_round rnd, const int32_t *src, void *d, size_t n, uint32_t *flags_out);
+CFT_API cft_status cft_cvt_from_u32(cft_device *dev, cft_format fmt, cft_round rnd, const uint32_t *src, void *d, size_t n, uint32_t *flags_out);
+CFT_API cft_status cft_cvt_from_i64(cft_device *dev, cft_format fmt, cft_round rnd, const int64_t *src, void *d, size_t n, uint32_t *flags_out);
+CFT_API cft_status cft_cvt_from_u64(cft_device *dev, cft_format fmt, cft_round rnd, const uint64_t *src, void *d, size_t n, uint32_t *flags_out);
+CFT_API cft_status cft_cvt_to_i32(cft_device *dev, cft_format fmt, cft_round rnd, int exact, const void *a, int32_t *dst, size_t n, uint32_t *flags_out);
+CFT_API cft_status cft_cvt_to_u32(cft_device *dev, cft_format fmt, cft_round rnd, int exact, const void *a, uint32_t *dst, size_t n, uint32_t *flags_out);
+CFT_API cft_status cft_cvt_to_i64(cft_device *dev, cft_format fmt, cft_round rnd, int exact, const void *a, int64_t *dst, size_t n, uint32_t *flags_out);
+CFT_API cft_status cft_cvt_to_u64(cft_device *dev, cft_format fmt, cft_round rnd, int exact, const void *a, uint64_t *dst, size_t n, uint32_t *flags_out);
+CFT_API cft_status cft_logb(cft_device *dev, cft_format fmt, const void *a, void *d, size_t n, uint32_t *flags_out);
+CFT_API cft_status cft_next_up(cft_device *dev, cft_format fmt, const void *a, void *d, size_t n, uint32_t *flags_out);
+CFT_API cft_status cft_next_down(cft_device *dev, cft_format fmt, const void *a, void *d, size_t n, uint32_t *flags_out);
+CFT_API cft_status cft_class(cft_device *dev, cft_format fmt, const void *a, uint8_t *cls, size_t n);
+CFT_API cft_status cft_total_order(cft_device *dev, cft_format fmt, const void *a, const void *b, void *d, size_t n);
+CFT_API cft_status cft_total_order_mag(cft_device *dev, cft_format fmt, const void *a, const void *b, void *d, size_t n);
+CFT_API cft_status cft_rem(cft_device *dev, cft_format fmt, const void *a, const void *b, void *d, size_t n, uint32_t *flags_out);
+/* the replay of the reference's published vector sets (cft.h:3397): the
+ * sets are the reference's, replayed by its own tests against this library */
+CFT_API cft_status cft_conformance(cft_device *dev, const char *dir, char *report, size_t report_size, uint64_t *cases_checked);
+
 #ifdef __cplusplus
 }
 #endif

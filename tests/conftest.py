@@ -6,6 +6,7 @@ import pytest
 ROOT = Path(__file__).resolve().parents[1]
 sys.path.insert(0, str(ROOT / "cft-fp256_gb300"))
 sys.path.insert(0, str(ROOT / "tests"))
+sys.path.insert(1, str(ROOT))              # bench_suites (benchmark and test workloads)
 
 
 def pytest_configure(config):

@@ -299,4 +299,6 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    sys.path.insert(0, str(Path(__file__).resolve().parents[1]))
+    from refpath import require_reference
+    main(require_reference(sys.argv))

@@ -4,7 +4,7 @@ python/cft_golden/softfloat.py (its compute(), div() and sqrt()).
 
 Run where the reference tree is present:
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py [REFERENCE_TREE]     # or CFT_REFERENCE
 
 The fixtures are committed; nothing at test time imports the reference.
 Cases: the seeded operand mix of cftgb.workload (specials, cancellation
@@ -68,4 +68,6 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    sys.path.insert(0, str(Path(__file__).resolve().parents[1]))
+    from refpath import require_reference
+    main(require_reference(sys.argv))

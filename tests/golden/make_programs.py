@@ -2,8 +2,8 @@
 reference itself, run here where its tree is present:
 
     make -C oracle ref                       # the reference library + cft-asm
-    python tests/golden/make_programs.py /root/reference
-    python tests/golden/make_programs.py /root/reference odes
+    python tests/golden/make_programs.py [REFERENCE_TREE]        # or CFT_REFERENCE
+    python tests/golden/make_programs.py REFERENCE_TREE odes
 
 For every program source the reference ships (programs/*.cfta and
 certificates/programs/*.cfta) it writes one .npz holding:
@@ -288,7 +288,9 @@ def main(ref):
 
 
 if __name__ == "__main__" and len(sys.argv) <= 2:
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    sys.path.insert(0, str(Path(__file__).resolve().parents[1]))
+    from refpath import require_reference
+    main(require_reference(sys.argv))
 
 
 def ode_banks(ref):

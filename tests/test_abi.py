@@ -127,3 +127,94 @@ def test_queue_block_shape_setter_checks_its_argument():
         assert L.cftg_queue_block_threads() == 128
     finally:
         L.cftg_set_queue_block_threads(before)
+
+# every function the reference's public header exports (host/include/cft.h,
+# its CFT_API declarations): the link-level interface a C caller binds
+REFERENCE_CFT_API = (
+    "cft_abi_version cft_acos cft_acosh cft_acospi cft_alloc cft_asin cft_asinh cft_asinpi "
+    "cft_atan cft_atan2 cft_atan2pi cft_atanh cft_atanpi cft_augmented_add cft_augmented_mul "
+    "cft_augmented_sub cft_buffer_data cft_buffer_free cft_buffer_from_device "
+    "cft_buffer_get_info cft_buffer_to_device cft_build_id cft_class cft_close cft_cmp_sig "
+    "cft_compound cft_conformance cft_convert cft_cos cft_cosh cft_cospi cft_cvt_from_i32 "
+    "cft_cvt_from_i64 cft_cvt_from_u32 cft_cvt_from_u64 cft_cvt_to_i32 cft_cvt_to_i64 "
+    "cft_cvt_to_u32 cft_cvt_to_u64 cft_div cft_exp cft_exp10 cft_exp10m1 cft_exp2 cft_exp2m1 "
+    "cft_expm1 cft_format_decimal_digits cft_format_name cft_format_size cft_formatof_add "
+    "cft_formatof_div cft_formatof_fma cft_formatof_mul cft_formatof_sqrt cft_formatof_sub "
+    "cft_from_decimal_char cft_from_hex_char cft_get_caps cft_get_image_id cft_get_payload "
+    "cft_hypot cft_is754version1985 cft_is754version2008 cft_is754version2019 cft_last_error "
+    "cft_log cft_log10 cft_log10p1 cft_log1p cft_log2 cft_log2p1 cft_logb cft_lower_flags "
+    "cft_max_mag cft_maxnum_mag cft_min_mag cft_minnum_mag cft_next_down cft_next_up "
+    "cft_op_name cft_open cft_open_ex cft_pow cft_pown cft_powr cft_program_digest "
+    "cft_program_free cft_program_get_info cft_program_load cft_program_run "
+    "cft_program_run_bank cft_program_run_ex cft_raise_flags cft_reduce cft_reduce_seg "
+    "cft_rem cft_restore_flags cft_rint cft_rootn cft_rsqrt cft_run cft_run_ex "
+    "cft_save_all_flags cft_scaleb cft_scaled_prod cft_scaled_prod_diff cft_scaled_prod_sum "
+    "cft_set_payload cft_set_payload_signaling cft_sha256 cft_sin cft_sinh cft_sinpi "
+    "cft_sqrt cft_strerror cft_supports cft_tan cft_tanh cft_tanpi cft_test_flags "
+    "cft_test_saved_flags cft_to_decimal_char cft_to_hex_char cft_total_order "
+    "cft_total_order_mag").split()
+
+
+def _public_names(text):
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return set(re.findall(r"CFT_API\s+[^;(]*?\b(cft_[a-z0-9_]+)\s*\(", text))
+
+
+def test_every_reference_entry_point_is_declared_and_exported():
+    """cft.h here (with the refusals it includes) declares, and the library
+    exports, every function the reference's cft.h exports."""
+    assert len(REFERENCE_CFT_API) == 125
+    ours = declared_symbols()
+    assert [n for n in REFERENCE_CFT_API if n not in ours] == []
+    L = cftgb.lib()
+    assert [n for n in REFERENCE_CFT_API if not hasattr(L, n)] == []
+
+
+def test_reference_header_names_are_the_frozen_list():
+    """Where the reference tree is present, its header still exports
+    exactly the names above (so the list is not stale)."""
+    from refpath import reference_root
+    ref = reference_root()
+    if ref is None:
+        pytest.skip("the reference tree is not present")
+    assert _public_names((ref / "host" / "include" / "cft.h").read_text()) == set(REFERENCE_CFT_API)
+
+
+def test_a_c_caller_of_every_entry_point_compiles_and_links(tmp_path):
+    """A C program that names every reference entry point, including cft.h
+    only, compiles against include/ and links against libcft_gb300.so."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    src = tmp_path / "caller.c"
+    body = ",\n".join(f"    (void (*)(void)){n}" for n in REFERENCE_CFT_API)
+    src.write_text('#include "cft.h"\n#include <stdio.h>\n'
+                   f"static void (*const table[])(void) = {{\n{body}\n}};\n"
+                   "int main(void) { printf(\"%zu %s\\n\", sizeof table / sizeof table[0], "
+                   "cft_strerror(CFT_OK)); return 0; }\n")
+    so = Path(cftgb.lib()._name)
+    exe = tmp_path / "caller"
+    p = subprocess.run([cc, "-std=c99", "-Wall", "-Werror", "-I", str(ROOT / "include"), str(src),
+                        "-o", str(exe), "-L", str(so.parent), "-lcft_gb300",
+                        f"-Wl,-rpath,{so.parent}"], capture_output=True, text=True)
+    assert p.returncode == 0, p.stderr
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0 and r.stdout.split() == ["125", "ok"], (r.stdout, r.stderr)
+
+
+def test_new_refusals_name_themselves():
+    L = cftgb.lib()
+    for name in ("cft_rint", "cft_convert", "cft_class", "cft_rem", "cft_cvt_to_u64",
+                 "cft_total_order_mag"):
+        fn = getattr(L, name)
+        fn.restype = ctypes.c_int
+        assert fn(None, 0, 0, 0, None, None, None, None, None) == 2, name
+        assert name.encode() in L.cft_last_error()
+    L.cft_conformance.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_char_p,
+                                  ctypes.c_size_t, ctypes.POINTER(ctypes.c_uint64)]
+    rep = ctypes.create_string_buffer(b"x" * 16)
+    cases = ctypes.c_uint64(99)
+    assert L.cft_conformance(None, None, rep, 16, ctypes.byref(cases)) == 2
+    assert rep.value == b"" and cases.value == 0

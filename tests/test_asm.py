@@ -25,12 +25,13 @@ import numpy as np
 import pytest
 
 from cftgb import asm
+from refpath import reference_root
 
 GOLDEN = Path(__file__).resolve().parent / "golden"
 CORPUS = json.load(gzip.open(GOLDEN / "asm_corpus.json.gz", "rt"))
 # the reference tree, where it is present (this checks against its own
 # definitions; the fixtures above carry the same checks everywhere else)
-REF = Path(os.environ.get("CFT_REFERENCE", "/root/reference"))
+REF = reference_root() or Path("/nonexistent-reference-tree")
 REF_TOOL = Path(__file__).resolve().parents[1] / "oracle" / "_ref" / "cft-asm"
 
 

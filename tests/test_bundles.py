@@ -11,7 +11,8 @@ import pytest
 import cftgb
 import oracle_lib
 import seq_util as su
-from cftgb import suites, workload as wl
+import bench_suites as suites
+from cftgb import workload as wl
 
 NOP = (1 << 64) - 1
 

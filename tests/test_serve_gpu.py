@@ -114,7 +114,7 @@ def test_program_requests_match_the_oracle(gpu, oracle):
 def test_mixed_requests_same_alone_and_in_the_mix(gpu):
     import torch
     L = cftgb.lib()
-    from cftgb import suites
+    import bench_suites as suites
     suites._bind(L)
     stream = torch.cuda.current_stream().cuda_stream
     rng = np.random.default_rng(21)

@@ -118,7 +118,7 @@ def test_group_launch_two_programs_two_formats(gpu, oracle, lane_threads):
     """Lorenz-63 at binary256 and Lorenz-96 at binary128, uneven run counts,
     as one graph launch (cftg_traj_group_*): every kept state's hash and
     every final state equal the oracle's segment-by-segment runs."""
-    from cftgb import suites
+    import bench_suites as suites
     z = np.load(su.GOLD / "odes.npz")
     progs = []
     for i, (key, fmt, slots, base, spr, lanes, every) in enumerate(

@@ -5,7 +5,9 @@ It serves callers that cannot let the library call cudaMalloc - a host
 whose device memory is all owned by its own pool or budget, or a loop that
 cannot take cudaMalloc's implicit synchronisation - so the run's scratch
 lives in a fixed array inside the library. The comparison is bit for bit
-(no tolerance): values, counts, deposits, flags and STATUS. Two calls in a
+(no tolerance): values, counts, deposits, flags and STATUS, against the
+ordinary run and against the reference library's own outputs for the same
+program and lanes (the committed fixture). Two calls in a
 row show that what the shared array kept from the first call does not leak
 into the second. This file sorts last so that a failure here stops a run
 only after every other test has run; it also passes alone.
@@ -86,10 +88,17 @@ def test_noalloc_matches_program_run_ex_twice(gpu, shape):
             torch.cuda.synchronize()
             got_sout = tsout.cpu().numpy().view(np.uint32)[: n * hd["sout"]]
             got_dep = tdep.cpu().numpy().view(np.uint32)[: n * hd["maxdep"]]
+            got_cnt = tcnt.cpu().numpy().view(np.uint32)
             assert np.array_equal(got_sout, want["scratch_out"]), f"call {call}: scratch-out"
             assert np.array_equal(got_dep, want["deposits"]), f"call {call}: deposits"
-            assert np.array_equal(tcnt.cpu().numpy().view(np.uint32), want["counts"]), f"call {call}"
+            assert np.array_equal(got_cnt, want["counts"]), f"call {call}"
             assert fl.value == want["flags"] and st.value == want["status"], f"call {call}"
+            # and the reference library's own outputs for the same lanes
+            # (the fixture, produced by its cft_program_run_ex)
+            assert np.array_equal(got_sout.reshape(-1), case["exp_scratch_out"].reshape(-1)), call
+            assert np.array_equal(got_dep.reshape(-1), case["exp_deposits"].reshape(-1)), call
+            assert np.array_equal(got_cnt, case["exp_counts"].astype(np.uint32)), call
+            assert fl.value == int(case["exp_flags"]) and st.value == int(case["exp_status"]), call
     finally:
         L.cft_program_free(prog)
 
