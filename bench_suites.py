@@ -52,8 +52,15 @@ def _bind(L):
     L.cftg_queue_block_threads.restype = ctypes.c_int
 
 
-def uneven(h, ncalls=10000, seed=4, max_log2=20, reps=3):
+def uneven(h, ncalls=10000, seed=4, max_log2=20, reps=3, sample=0, timed=None):
+    """The uneven batch, plain per-call launches against the batched form.
+    `timed` (a context manager, e.g. a clock sampler) wraps the timed
+    loops. With sample > 0 the result also carries, under "_samples", the
+    first and last `sample` elements of every call (operands, the batched
+    form's results) and every call's flag word, for the oracle."""
+    import contextlib
     import torch
+    timed = timed if timed is not None else contextlib.nullcontext()
     L = _lib.lib()
     _bind(L)
     rng = np.random.default_rng(seed)
@@ -120,6 +127,7 @@ def uneven(h, ncalls=10000, seed=4, max_log2=20, reps=3):
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     plain_ms = []
+    timed.__enter__()
     for _ in range(reps):
         flags_plain.zero_()
         torch.cuda.synchronize()
@@ -136,13 +144,46 @@ def uneven(h, ncalls=10000, seed=4, max_log2=20, reps=3):
         e1.record(s2)
         s2.synchronize()
         q_ms.append(e0.elapsed_time(e1))
+    timed.__exit__(None, None, None)
     exact = all(torch.equal(arena[f]["d1"], arena[f]["d2"]) for f in (1, 2, 3)) and \
         torch.equal(flags_plain, flags_q)
     tiles = L.cftg_batch_tiles(batch)
     L.cftg_batch_free(batch)
+    samples = None
+    if sample:
+        # each call's head and tail (its ragged last tile included), gathered
+        # per format with one index_select a buffer
+        esz_w = {f: esz[f] // 4 for f in (1, 2, 3)}
+        starts = {1: 0, 2: 0, 3: 0}
+        rows = {f: [] for f in (1, 2, 3)}
+        taken = {1: 0, 2: 0, 3: 0}
+        spans = []
+        for i in range(ncalls):
+            f, n = int(fmts[i]), int(sizes[i])
+            s0 = starts[f]
+            starts[f] += n
+            idx = np.arange(n) if n <= 2 * sample else np.r_[0:sample, n - sample:n]
+            spans.append((f, taken[f], len(idx), n))
+            taken[f] += len(idx)
+            rows[f].append(s0 + idx)
+        got = {}
+        for f in (1, 2, 3):
+            if not rows[f]:
+                continue
+            ti = torch.from_numpy(np.concatenate(rows[f]).astype(np.int64)).cuda()
+            got[f] = {k: arena[f][k].view(-1, esz_w[f]).index_select(0, ti).cpu().numpy()
+                      .view(np.uint32) for k in ("a", "b", "c", "d2")}
+        fq = flags_q.cpu().numpy().view(np.uint32)
+        samples = []
+        for i, (f, r0, k, n) in enumerate(spans):
+            kind, op = kinds[int(which[i])]
+            g = got[f]
+            samples.append(dict(kind=kind, op=op, fmt=f, rnd=int(rnds[i]), n=n, whole=k == n,
+                                a=g["a"][r0:r0 + k], b=g["b"][r0:r0 + k], c=g["c"][r0:r0 + k],
+                                d=g["d2"][r0:r0 + k], flags=int(fq[i])))
     total = int(sizes.sum())
     pm, qm = min(plain_ms), min(q_ms)
-    return {
+    out = {
         "suite": "uneven", "calls": ncalls, "elements": total,
         "plain_ms": pm, "batched_ms": qm, "speedup": pm / qm,
         "plain_gelem_s": total / pm / 1e6, "batched_gelem_s": total / qm / 1e6,
@@ -151,6 +192,9 @@ def uneven(h, ncalls=10000, seed=4, max_log2=20, reps=3):
                          for f in (1, 2, 3)},
         "block_threads": int(L.cftg_queue_block_threads()),
     }
+    if samples is not None:
+        out["_samples"] = samples
+    return out
 
 
 TAG = b"cft-certificate 1 state\0"
@@ -202,7 +246,7 @@ def state_hashes(snaps, runs, snap_every, max_snaps, slots, W):
     return per_lane, outer.hexdigest()
 
 
-def trajectories(h, progs, reps=2, separate=False):
+def trajectories(h, progs, reps=2, separate=False, timed=None):
     """progs: a list of dicts with image, bank (uint8 arrays), fmt, slots,
     init (lane-major uint32 blocks), runs (uint32 per lane), snap_every,
     max_snaps, steps_per_run. Runs them all as one graph launch, `reps`
@@ -245,15 +289,19 @@ def trajectories(h, progs, reps=2, separate=False):
                "cftg_traj_group_capture")
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     times = []
+    import contextlib
     for _ in range(reps):
         for t in keep:
             t["state"].copy_(t["init"])
             t["snaps"].zero_()
+            t["lf"].zero_()
         torch.cuda.synchronize()
-        e0.record(stream)
-        _lib.check(L.cftg_traj_group_launch(group, stream.cuda_stream), "cftg_traj_group_launch")
-        e1.record(stream)
-        stream.synchronize()
+        with (timed if timed is not None else contextlib.nullcontext()):
+            e0.record(stream)
+            _lib.check(L.cftg_traj_group_launch(group, stream.cuda_stream),
+                       "cftg_traj_group_launch")
+            e1.record(stream)
+            stream.synchronize()
         times.append(e0.elapsed_time(e1) / 1e3)
     out = {"suite": "trajectories", "launch_s": min(times), "launches": reps, "programs": []}
     if separate:
@@ -289,7 +337,8 @@ def trajectories(h, progs, reps=2, separate=False):
             "max_steps": int(np.max(P["runs"])) * P["steps_per_run"],
             "flags": fl.value, "status": st.value, "state_hash_digest": digest,
             "final_digest": hashlib.sha256(TAG + final.tobytes()).hexdigest(),
-            "_final": final, "_hashes": per_lane})
+            "_final": final, "_hashes": per_lane,
+            "_lane_flags": t["lf"].cpu().numpy().copy()})
     L.cftg_traj_group_free(group)
     for t in keep:
         L.cftg_traj_free(t["traj"])
@@ -303,13 +352,18 @@ SWEEP_OPS = (("add", 0, 1), ("sub", 0, 2), ("mul", 0, 3), ("fma", 0, 0), ("div",
              ("sqrt", 2, 0))
 
 
-def sweep(h, n=1 << 24, reps=3, check_n=4096, seed=11):
+def sweep(h, n=1 << 24, reps=3, seed=11, check=None, spread=1 << 20, timed=None):
     """The elementwise sweep: every format x {add, sub, mul, fma, div, sqrt}
     x rounding attribute over n device-generated operands a cell (the
-    benchmark's value mix). Each cell is timed over `reps` launches with CUDA
-    events; the cell is run once more with per-element flag bytes and a
-    prefix of check_n elements is returned (operands, results, flags) for
-    the oracle."""
+    benchmark's value mix, with exact-cancellation triples and halfway cases
+    planted). Each cell is timed over `reps` launches with CUDA events
+    (inside `timed`, a context manager such as a clock sampler); the cell is
+    run once more with per-element flag bytes and, when `check` is given,
+    handed to it: check(cell, operands, results, flag bytes) with host
+    arrays of every element for add/sub/mul/fma and of `spread` elements
+    spread evenly over the array (first and last included) for div and
+    sqrt. check returns a dict merged into the cell."""
+    import contextlib
     import torch
     from cftgb import workload as wl
     L = _lib.lib()
@@ -318,15 +372,22 @@ def sweep(h, n=1 << 24, reps=3, check_n=4096, seed=11):
     s = stream.cuda_stream
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     word = torch.zeros(1, dtype=torch.int32, device="cuda")
-    cells, checks = [], []
+    cells = []
+    pick = np.unique(np.linspace(0, n - 1, min(n, spread)).astype(np.int64))
+    tpick = torch.from_numpy(pick).cuda()
     for fmt in range(4):
         W = wl.words(fmt)
         ops = [torch.empty(n * W, dtype=torch.int32, device="cuda") for _ in range(4)]
         for j in range(3):
             _lib.check(L.cftg_fill_operands(fmt, ops[j].data_ptr(), n, seed * 16 + fmt * 4 + j, 64,
                                             100000, s), "cftg_fill_operands")
+        wl.plant(fmt, ops[:3], n, seed * 16 + fmt)
         lf = torch.zeros(n, dtype=torch.uint8, device="cuda")
         pa, pb, pc, pd = (x.data_ptr() for x in ops)
+        host_all = host_pick = None
+        if check is not None:
+            host_all = [x.cpu().numpy().view(np.uint32).reshape(n, W) for x in ops[:3]]
+            host_pick = [x[pick] for x in host_all]
         for name, kind, op in SWEEP_OPS:
             for rnd in range(5):
                 def go(nn, lfp):
@@ -335,23 +396,35 @@ def sweep(h, n=1 << 24, reps=3, check_n=4096, seed=11):
                     _lib.check(st, "cftg_run_device")
                 go(n, None)
                 torch.cuda.synchronize()
-                e0.record(stream)
-                for _ in range(reps):
-                    go(n, None)
-                e1.record(stream)
-                torch.cuda.synchronize()
+                with (timed if timed is not None else contextlib.nullcontext()):
+                    e0.record(stream)
+                    for _ in range(reps):
+                        go(n, None)
+                    e1.record(stream)
+                    torch.cuda.synchronize()
                 ms = e0.elapsed_time(e1) / reps
-                cells.append({"fmt": ("fp32", "fp64", "fp128", "fp256")[fmt], "op": name,
-                              "rnd": rnd, "ms": ms, "gelem_s": n / ms / 1e6})
-                # the checked prefix comes from a full-size launch (the kernel
-                # the cell timed), with per-element flag bytes
-                go(n, lf.data_ptr())
-                torch.cuda.synchronize()
-                host = [x[:check_n * W].cpu().numpy().view(np.uint32).reshape(-1, W) for x in ops]
-                checks.append(dict(fmt=fmt, kind=kind, op=op, rnd=rnd, a=host[0], b=host[1],
-                                   c=host[2], d=host[3], lf=lf[:check_n].cpu().numpy().copy()))
-        del ops
-    return {"suite": "sweep", "elements_per_cell": n, "cells": cells, "_checks": checks}
+                cell = {"fmt": ("fp32", "fp64", "fp128", "fp256")[fmt], "op": name, "rnd": rnd,
+                        "ms": ms, "gelem_s": n / ms / 1e6}
+                if check is not None:
+                    # the checked results come from a full-size launch (the
+                    # kernel the cell timed), with per-element flag bytes
+                    word.zero_()
+                    go(n, lf.data_ptr())
+                    torch.cuda.synchronize()
+                    d = ops[3].view(n, W)
+                    if kind == 0:
+                        hd, hl, hops = d.cpu().numpy().view(np.uint32), lf.cpu().numpy(), host_all
+                    else:
+                        hd = d.index_select(0, tpick).cpu().numpy().view(np.uint32)
+                        hl, hops = lf.index_select(0, tpick).cpu().numpy(), host_pick
+                    cell.update(check(dict(fmt=fmt, kind=kind, op=op, rnd=rnd,
+                                           word=int(word.item()) & 0x1F, whole=kind == 0),
+                                      hops, hd, hl))
+                cells.append(cell)
+        del ops, host_all, host_pick
+        torch.cuda.empty_cache()
+    return {"suite": "sweep", "elements_per_cell": n, "spread_checked": int(len(pick)),
+            "cells": cells}
 
 
 def hh_init(lanes, seed):
@@ -376,7 +449,7 @@ def hh_init(lanes, seed):
 def serving(h, hh_image, hh_bank, rate=20000.0, seconds=60.0, seed=5, budget=40 << 30,
             program_frac=0.02, hh_lanes=32, max_log2=22, sample_every=2000, max_inflight=6,
             max_program_inflight=2, max_batch_elements=1 << 24, elem_blocks_per_sm=0,
-            sample_max_n=1 << 20):
+            sample_max_n=1 << 20, timed=None):
     """Open-loop serving: requests arrive as a Poisson stream of `rate` a
     second for `seconds`; each is an element call (binary128 or binary256
     1:1, size log-uniform in [64, 2^max_log2], operation uniform over add,
@@ -390,8 +463,10 @@ def serving(h, hh_image, hh_bank, rate=20000.0, seconds=60.0, seed=5, budget=40 
     before the stream starts, for the comparison with the same request run
     alone: pinning memory while requests arrive would stall the submitting
     thread and charge the stall to the requests behind it."""
+    import contextlib
     import torch
     from cftgb import serving as sv
+    timed = timed if timed is not None else contextlib.nullcontext()
     from cftgb import workload as wl
     L = _lib.lib()
     _bind(L)
@@ -451,7 +526,7 @@ def serving(h, hh_image, hh_bank, rate=20000.0, seconds=60.0, seed=5, budget=40 
     with sv.Server(h, budget, max_inflight=max_inflight, max_program_inflight=max_program_inflight,
                    max_batch_calls=4096, max_batch_lanes=1 << 16,
                    max_batch_elements=max_batch_elements,
-                   elem_blocks_per_sm=elem_blocks_per_sm) as srv:
+                   elem_blocks_per_sm=elem_blocks_per_sm) as srv, timed:
         t0 = sv.clock_ns() + 20_000_000
         arr_ns = (t0 + arrive * 1e9).astype(np.int64)
         i = loops = 0

@@ -186,3 +186,65 @@ def encode_double(fmt, x):
     else:
         sig, e2 = frac | (1 << 52), e - 1023 - 52
     return encode(fmt, sign, sig, e2)
+
+
+def hard_rows(fmt, m, seed):
+    """m operand rows (a, b, c), each (m, W) uint32, that are all hard cases
+    of the value mix: the first half exact-cancellation triples (a*b exact,
+    c = -(a*b)); then, alternately, a*b with exactly p+1 significant bits and
+    its last bit set with c = +-0 (a tie for MUL and FMA) and a + c with c
+    exactly half an ulp of a and b = 1.0 (a tie for ADD and SUB). Planted
+    into device-generated arrays (plant()), they give those arrays the mix
+    gen_operands() gives host arrays, at sizes where building every row on
+    the host would take minutes."""
+    g = geometry(fmt)
+    W, p = g["W"], g["prec"]
+    rng = np.random.default_rng(seed)
+    a = np.zeros((m, W), np.uint32)
+    b = np.zeros((m, W), np.uint32)
+    c = np.zeros((m, W), np.uint32)
+    h = p // 2
+    for i in range(m):
+        if i < m // 2:
+            sa, sb = _rand_bits(rng, h) | 1, _rand_bits(rng, h) | 1
+            ea, eb = int(rng.integers(-40, 40)), int(rng.integers(-40, 40))
+            s1, s2 = int(rng.integers(0, 2)), int(rng.integers(0, 2))
+            a[i] = from_int(encode(fmt, s1, sa, ea), W)
+            b[i] = from_int(encode(fmt, s2, sb, eb), W)
+            c[i] = from_int(encode(fmt, 1 - (s1 ^ s2), sa * sb, ea + eb), W)
+        elif i % 2 == 0:
+            for _ in range(64):
+                ka = int(rng.integers(2, p))
+                sa = _rand_bits(rng, ka) | 1
+                sb = _rand_bits(rng, p + 2 - ka) | 1
+                if (sa * sb).bit_length() == p + 1:
+                    break
+            a[i] = from_int(encode(fmt, int(rng.integers(0, 2)), sa, int(rng.integers(-30, 30))), W)
+            b[i] = from_int(encode(fmt, int(rng.integers(0, 2)), sb, int(rng.integers(-30, 30))), W)
+            c[i, W - 1] = np.uint32(int(rng.integers(0, 2)) << 31)              # +-0
+        else:
+            ea = int(rng.integers(-30, 30))
+            a[i] = from_int(encode(fmt, int(rng.integers(0, 2)), _rand_bits(rng, p), ea), W)
+            c[i] = from_int(encode(fmt, int(rng.integers(0, 2)), 1, ea - 1), W)
+            b[i] = from_int(encode(fmt, 0, 1, 0), W)                            # 1.0
+    return a, b, c
+
+
+def plant(fmt, tensors, n, seed, frac=0.045, rows=8192):
+    """Write hard_rows() (cycled) over a fraction `frac` of the n elements of
+    three device operand tensors (torch, n*W int32 each) at seeded distinct
+    positions; returns the positions (sorted int64)."""
+    import torch
+    W = words(fmt)
+    hr = hard_rows(fmt, rows, seed)
+    rng = np.random.default_rng(seed + 1)
+    k = min(n, int(n * frac))
+    if k == 0:
+        return np.zeros(0, np.int64)
+    pos = np.sort(rng.choice(n, size=k, replace=False)).astype(np.int64)
+    which = rng.integers(0, rows, size=k)
+    ti = torch.from_numpy(pos).to(tensors[0].device)
+    for t, h in zip(tensors, hr):
+        src = torch.from_numpy(np.ascontiguousarray(h[which]).view(np.int32)).to(t.device)
+        t.view(-1, W).index_copy_(0, ti, src)
+    return pos
