@@ -396,19 +396,16 @@ SFD void fma_general(const Unp<FMT> &ua, const Unp<FMT> &ub, const Unp<FMT> &uc,
     round_pack<FMT, N, OP != OP_MUL>(rs, P, ew, rnd, out, flags);
 }
 
-// One element of FMA/ADD/SUB/MUL. x/y/z are the caller's a, b, c (b unused
-// for ADD/SUB, c unused for MUL). Special cases follow the reference's
-// order (host/src/softfloat.c:335-373).
+// The steered operands of FMA/ADD/SUB/MUL, unpacked: x/y/z are the
+// caller's a, b, c (b unused for ADD/SUB, c unused for MUL); csteer is the
+// steered addend's encoding (host/src/softfloat.c:438-468).
 template <int FMT, int OP>
-SFD void arith(const uint32_t (&x)[Fmt<FMT>::W], const uint32_t (&y)[Fmt<FMT>::W],
-               const uint32_t (&z)[Fmt<FMT>::W], int rnd, uint32_t (&out)[Fmt<FMT>::W],
-               uint32_t &flags)
+SFD void steer_unpack(const uint32_t (&x)[Fmt<FMT>::W], const uint32_t (&y)[Fmt<FMT>::W],
+                      const uint32_t (&z)[Fmt<FMT>::W], Unp<FMT> &ua, Unp<FMT> &ub,
+                      Unp<FMT> &uc, uint32_t (&csteer)[Fmt<FMT>::W])
 {
-    using F = Fmt<FMT>;
-    constexpr int W = F::W;
-    Unp<FMT> ua, ub, uc;
-    uint32_t bsteer[W], csteer[W];
-    // steering
+    constexpr int W = Fmt<FMT>::W;
+    uint32_t bsteer[W];
     if constexpr (OP == OP_ADD || OP == OP_SUB) {
         enc_one<FMT>(bsteer, 0);
     } else {
@@ -425,37 +422,85 @@ SFD void arith(const uint32_t (&x)[Fmt<FMT>::W], const uint32_t (&y)[Fmt<FMT>::W
     unpack<FMT, 32 * W - 2>(x, ua);
     unpack<FMT, 32 * W - 1>(bsteer, ub);
     unpack<FMT, 32 * W - 2>(csteer, uc);
-    flags = 0u;
+}
 
+// The special cases in the reference's order (host/src/softfloat.c:335-373):
+// true, with the result and flags, when an operand is a NaN or an infinity
+// or a factor is zero; false when the element needs fma_general.
+template <int FMT>
+SFD bool arith_special_case(const Unp<FMT> &ua, const Unp<FMT> &ub, const Unp<FMT> &uc,
+                            const uint32_t (&csteer)[Fmt<FMT>::W], int rnd,
+                            uint32_t (&out)[Fmt<FMT>::W], uint32_t &flags)
+{
+    constexpr int W = Fmt<FMT>::W;
+    flags = 0u;
     if (ua.cls == C_NAN || ub.cls == C_NAN || uc.cls == C_NAN) {
         enc_qnan<FMT>(out);
         flags = any_snan(ua, ub, uc) ? F_INVALID : 0u;
-        return;
+        return true;
     }
     const int sp = ua.sign ^ ub.sign;
     if (ua.cls == C_INF || ub.cls == C_INF) {
         if (ua.cls == C_ZERO || ub.cls == C_ZERO || (uc.cls == C_INF && uc.sign != sp)) {
             enc_qnan<FMT>(out);                    // inf * 0, inf - inf
             flags = F_INVALID;
-            return;
+            return true;
         }
         enc_inf<FMT>(out, sp);
-        return;
+        return true;
     }
     if (uc.cls == C_INF) {
         enc_inf<FMT>(out, uc.sign);
-        return;
+        return true;
     }
     if (ua.cls == C_ZERO || ub.cls == C_ZERO) {
         if (uc.cls == C_ZERO) {
             enc_zero<FMT>(out, uc.sign == sp ? uc.sign : (rnd == RDN ? 1 : 0));
-            return;
+            return true;
         }
 #pragma unroll
         for (int i = 0; i < W; i++) out[i] = csteer[i];   // 0*b + c is c, exactly
-        return;
+        return true;
     }
+    return false;
+}
+
+// One element of FMA/ADD/SUB/MUL: the special cases, else the general path.
+template <int FMT, int OP>
+SFD void arith(const uint32_t (&x)[Fmt<FMT>::W], const uint32_t (&y)[Fmt<FMT>::W],
+               const uint32_t (&z)[Fmt<FMT>::W], int rnd, uint32_t (&out)[Fmt<FMT>::W],
+               uint32_t &flags)
+{
+    Unp<FMT> ua, ub, uc;
+    uint32_t csteer[Fmt<FMT>::W];
+    steer_unpack<FMT, OP>(x, y, z, ua, ub, uc, csteer);
+    if (arith_special_case<FMT>(ua, ub, uc, csteer, rnd, out, flags)) return;
     fma_general<FMT, OP>(ua, ub, uc, uc.sign, rnd, out, flags);
+}
+
+// Whether an element of FMA/ADD/SUB/MUL takes arith_special_case (a NaN or
+// an infinity among the steered operands, or a zero factor), from the
+// encodings' exponent fields and fraction bits alone.
+template <int FMT, int OP>
+SFD bool arith_is_special(const uint32_t (&x)[Fmt<FMT>::W], const uint32_t (&y)[Fmt<FMT>::W],
+                          const uint32_t (&z)[Fmt<FMT>::W])
+{
+    constexpr int W = Fmt<FMT>::W;
+    constexpr uint32_t FRAC_TOP = (1u << exp_shift<FMT>()) - 1u;
+    auto frac_zero = [](const uint32_t (&v)[W]) {
+        uint32_t o = v[W - 1] & FRAC_TOP;
+#pragma unroll
+        for (int i = 0; i < W - 1; i++) o |= v[i];
+        return o == 0u;
+    };
+    const uint32_t ex = exp_field<FMT>(x);
+    bool sp = ex == exp_mask<FMT>() || (ex == 0u && frac_zero(x));       // a: NaN, inf, zero
+    if constexpr (OP == OP_FMA || OP == OP_MUL) {
+        const uint32_t ey = exp_field<FMT>(y);
+        sp = sp || ey == exp_mask<FMT>() || (ey == 0u && frac_zero(y));   // b: NaN, inf, zero
+    }
+    if constexpr (OP != OP_MUL) sp = sp || exp_field<FMT>(z) == exp_mask<FMT>();   // c: NaN, inf
+    return sp;
 }
 
 // FMA/ADD/SUB/MUL with the operation chosen at run time, all through the one

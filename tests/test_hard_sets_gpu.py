@@ -77,11 +77,11 @@ def test_wide_encodings_and_near_overflow_sums_through_reductions(gpu, oracle, f
             assert oracle.L.sfp_reduce(fmt, op, 0, a2.ctypes.data, b2.ctypes.data, rd.ctypes.data,
                                        t, ctypes.byref(rfl)) == 0
             assert np.array_equal(d, rd) and fl.value == rfl.value, (op, t, "near max")
-        # segmented, over the same wide encodings
-        n = 4096
-        a, b = _wide(fmt, n, 777 + fmt)
+        # segmented, over wide encodings
         for seg in (1, 3, 32, 96, 1024):
-            m = n // seg
+            m = 4096 // seg
+            n = m * seg                       # whole segments
+            a, b = _wide(fmt, n, 777 + fmt + seg)
             d, fl = np.zeros((m, W), np.uint32), ctypes.c_uint32()
             assert L.cft_reduce_seg(gpu, op, fmt, 3, a.ctypes.data,
                                     b.ctypes.data if op == 25 else None, d.ctypes.data, n, seg,
