@@ -47,15 +47,10 @@ cudaError_t launch_elem(const ElemLaunch &L, cudaStream_t stream);
 // status and the result true); false when the direct kernels take L.
 bool launch_elem_bulk(const ElemLaunch &L, cudaStream_t stream, cudaError_t *err);
 
-// Binary32/64 FMA/ADD/SUB/MUL under RNE/RTZ/RDN/RUP on the hardware's
+// Binary32 FMA/ADD/SUB/MUL under RNE/RTZ/RDN/RUP on the hardware's
 // rounding, with the elements it cannot take on the integer path
 // (elem_hw.cu): true (and *err its status) when it takes L.
 bool launch_elem_hw(const ElemLaunch &L, cudaStream_t stream, cudaError_t *err);
-
-// Binary128/256 FMA/ADD/SUB/MUL with special elements sorted out of the
-// general path's warps (elem_q.cu): true (and *err its status) when it
-// takes L.
-bool launch_elem_q(const ElemLaunch &L, cudaStream_t stream, cudaError_t *err);
 
 // The kernels' dimensions for a given launch (used by the queue autotuner).
 int sm_count();

@@ -75,13 +75,11 @@ cudaError_t launch_elem(const ElemLaunch &L, cudaStream_t s)
 {
     if (L.n == 0) return cudaSuccess;
     // the staged kernels when asked for (CFTG_ELEM_STAGING=bulk); else
-    // binary32/64 arithmetic on the hardware's rounding (elem_hw.cu),
-    // binary128/256 arithmetic with specials sorted out (elem_q.cu), and the
+    // binary32 arithmetic on the hardware's rounding (elem_hw.cu), and the
     // one-element-a-thread kernels here for everything else
     cudaError_t err = cudaSuccess;
     if (launch_elem_bulk(L, s, &err)) return err;
     if (launch_elem_hw(L, s, &err)) return err;
-    if (launch_elem_q(L, s, &err)) return err;
     switch (L.fmt) {
     case 0: return go_fmt<0>(L, s);
     case 1: return go_fmt<1>(L, s);

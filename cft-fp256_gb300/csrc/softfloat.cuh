@@ -361,7 +361,8 @@ SFD void fma_general(const Unp<FMT> &ua, const Unp<FMT> &ub, const Unp<FMT> &uc,
                 }
             }
         }
-        sfw::shr_jam_imad(X, pbig ? -delta : delta);
+        if constexpr (N >= 16) sfw::shr_jam_imad_far(X, pbig ? -delta : delta);
+        else sfw::shr_jam_imad(X, pbig ? -delta : delta);
         if (!pbig) ew += delta;
         const int s_big = pbig ? sp : sc, s_small = pbig ? sc : sp;
         // Y + X, or Y - X in two's complement, then the magnitude.
@@ -476,31 +477,6 @@ SFD void arith(const uint32_t (&x)[Fmt<FMT>::W], const uint32_t (&y)[Fmt<FMT>::W
     steer_unpack<FMT, OP>(x, y, z, ua, ub, uc, csteer);
     if (arith_special_case<FMT>(ua, ub, uc, csteer, rnd, out, flags)) return;
     fma_general<FMT, OP>(ua, ub, uc, uc.sign, rnd, out, flags);
-}
-
-// Whether an element of FMA/ADD/SUB/MUL takes arith_special_case (a NaN or
-// an infinity among the steered operands, or a zero factor), from the
-// encodings' exponent fields and fraction bits alone.
-template <int FMT, int OP>
-SFD bool arith_is_special(const uint32_t (&x)[Fmt<FMT>::W], const uint32_t (&y)[Fmt<FMT>::W],
-                          const uint32_t (&z)[Fmt<FMT>::W])
-{
-    constexpr int W = Fmt<FMT>::W;
-    constexpr uint32_t FRAC_TOP = (1u << exp_shift<FMT>()) - 1u;
-    auto frac_zero = [](const uint32_t (&v)[W]) {
-        uint32_t o = v[W - 1] & FRAC_TOP;
-#pragma unroll
-        for (int i = 0; i < W - 1; i++) o |= v[i];
-        return o == 0u;
-    };
-    const uint32_t ex = exp_field<FMT>(x);
-    bool sp = ex == exp_mask<FMT>() || (ex == 0u && frac_zero(x));       // a: NaN, inf, zero
-    if constexpr (OP == OP_FMA || OP == OP_MUL) {
-        const uint32_t ey = exp_field<FMT>(y);
-        sp = sp || ey == exp_mask<FMT>() || (ey == 0u && frac_zero(y));   // b: NaN, inf, zero
-    }
-    if constexpr (OP != OP_MUL) sp = sp || exp_field<FMT>(z) == exp_mask<FMT>();   // c: NaN, inf
-    return sp;
 }
 
 // FMA/ADD/SUB/MUL with the operation chosen at run time, all through the one

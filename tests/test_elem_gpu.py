@@ -128,8 +128,8 @@ def test_aliasing_and_null_operands(gpu, oracle):
     assert e.value.status == 1
 
 
-def test_run_ex_scalar_and_index_tables(gpu, oracle):
-    fmt = 3
+@pytest.mark.parametrize("fmt", [0, 1, 3])
+def test_run_ex_scalar_and_index_tables(gpu, oracle, fmt):
     n = 3000
     a, b, c = wl.gen_operands(fmt, n, 9)
     d = np.zeros_like(a)
