@@ -72,6 +72,118 @@ Access access_of(uint64_t w)
     return a;
 }
 
+// A micro-operation of a stretch before scheduling: its word (the layout
+// of BundleSchedule::ops), the locations it reads and the one it writes.
+struct UOp { uint64_t word; int reads[3]; int nreads; int write; };
+
+constexpr uint64_t U_MOVE = 1ull << 14, U_NEG_C = 1ull << 15;
+constexpr int OP_NEG = 5;
+
+int ufield(uint64_t w, int shift) { return (int)((w >> shift) & 0xFFFu); }
+
+uint64_t uset(uint64_t w, int shift, int loc)
+{
+    return (w & ~(0xFFFull << shift)) | ((uint64_t)(loc & 0xFFF) << shift);
+}
+
+// The locations a micro-operation reads, from its word.
+void reads_of(UOp &u)
+{
+    u.nreads = 0;
+    if (u.word & U_MOVE) {
+        u.reads[u.nreads++] = ufield(u.word, 28);
+        return;
+    }
+    const unsigned need = op_operands((int)(u.word & 0xFF));
+    for (int k = 0; k < 3; k++)
+        if (((need >> k) & 1u) && !((u.word >> (11 + k)) & 1u)) u.reads[u.nreads++] = ufield(u.word, 28 + 12 * k);
+}
+
+// Two rewrites of a stretch's micro-operations that shorten its schedule's
+// dependence chains and leave every location's value where and when the
+// plain program would have it:
+//  1. A NEG (a sign flip: exact, no flags, NaN payloads kept) read as a
+//     later operation's operand c is folded into that read: the operation
+//     reads the NEG's own operand with bit U_NEG_C, and flips the sign bit
+//     itself. The operation no longer waits for the NEG; a NEG whose value
+//     nothing reads any more is dropped.
+//  2. The value a stretch leaves in a register or slot is written there by
+//     its producer instead of by a MOVE at the stretch's end, when nothing
+//     after the producer (in program order) reads that location's value
+//     from before the stretch; the list scheduler then keeps the producer
+//     at or after the earlier readers of that old value (a bundle reads all
+//     its operands before any result is written).
+void rewrite_stretch(std::vector<UOp> &list, std::vector<char> &dead, int arch, int nloc)
+{
+    const size_t n = list.size();
+    std::vector<int> prod(nloc, -1);
+    for (size_t i = 0; i < n; i++)
+        if (list[i].write >= arch) prod[list[i].write] = (int)i;     // temps: written once
+    // 1. NEG folded into operand c
+    for (size_t i = 0; i < n; i++) {
+        UOp &u = list[i];
+        const uint64_t w = u.word;
+        if ((w & (U_MOVE | U_NEG_C)) || !((op_operands((int)(w & 0xFF)) >> 2) & 1u) || ((w >> 13) & 1u))
+            continue;
+        const int v = ufield(w, 52);
+        if (v < arch || prod[v] < 0) continue;
+        const uint64_t nw = list[prod[v]].word;
+        if ((nw & U_MOVE) || (int)(nw & 0xFF) != OP_NEG) continue;
+        u.word = uset(w, 52, ufield(nw, 28)) | (((nw >> 11) & 1ull) << 13) | U_NEG_C;
+        reads_of(u);
+    }
+    std::vector<int> readers(nloc, 0);
+    for (size_t i = 0; i < n; i++)
+        for (int k = 0; k < list[i].nreads; k++) readers[list[i].reads[k]]++;
+    for (size_t i = 0; i < n; i++) {
+        const uint64_t w = list[i].word;
+        if (!(w & U_MOVE) && (int)(w & 0xFF) == OP_NEG && list[i].write >= arch && !readers[list[i].write]) {
+            dead[i] = 1;
+            for (int k = 0; k < list[i].nreads; k++) readers[list[i].reads[k]]--;
+        }
+    }
+    // 2. the stretch's end MOVEs folded into their values' producers
+    std::vector<int> into(nloc, -1);                   // temp -> the location it now writes
+    for (size_t m = 0; m < n; m++) {
+        UOp &mv = list[m];
+        if (dead[m] || !(mv.word & U_MOVE) || mv.write >= arch) continue;
+        const int loc = mv.write, v = ufield(mv.word, 28);
+        if (v < arch) continue;
+        if (into[v] >= 0) {                            // already lives in another home
+            mv.word = uset(mv.word, 28, into[v]);
+            reads_of(mv);
+            continue;
+        }
+        const int p = prod[v];
+        if (p < 0 || dead[p]) continue;
+        bool later_read = false;
+        for (size_t j = (size_t)p + 1; j < n && !later_read; j++) {
+            if (dead[j] || j == m) continue;
+            for (int k = 0; k < list[j].nreads; k++)
+                if (list[j].reads[k] == loc) later_read = true;
+        }
+        if (later_read) continue;
+        list[p].word = uset(list[p].word, 16, loc);
+        list[p].write = loc;
+        for (size_t j = (size_t)p + 1; j < n; j++) {
+            if (dead[j]) continue;
+            UOp &u = list[j];
+            bool hit = false;
+            for (int k = 0; k < 3; k++) {
+                const int sh = 28 + 12 * k;
+                const bool isloc = (u.word & U_MOVE) ? k == 0 : !((u.word >> (11 + k)) & 1u);
+                if (isloc && ufield(u.word, sh) == v) {
+                    u.word = uset(u.word, sh, loc);
+                    hit = true;
+                }
+            }
+            if (hit) reads_of(u);
+        }
+        into[v] = loc;
+        dead[m] = 1;
+    }
+}
+
 }  // namespace
 
 // Schedule `insns` for G threads a lane. False when the program has an
@@ -99,7 +211,6 @@ bool build_bundles(const std::vector<uint64_t> &insns, uint32_t reach, int G, Bu
     int temps_max = 0;
     bool too_big = false;
 
-    struct UOp { uint64_t word; int reads[3]; int nreads; int write; };
     auto uop = [](int op, int rnd, bool move, int dest, const int src[3], const bool kst[3]) {
         uint64_t w = (uint64_t)(op & 0xFF) | ((uint64_t)(rnd & 7) << 8) |
                      ((uint64_t)kst[0] << 11) | ((uint64_t)kst[1] << 12) | ((uint64_t)kst[2] << 13) |
@@ -175,12 +286,16 @@ bool build_bundles(const std::vector<uint64_t> &insns, uint32_t reach, int G, Bu
         }
         temps_max = std::max(temps_max, next - arch);
         if (next > 4095) too_big = true;
+        std::vector<char> dead(list.size(), 0);
+        rewrite_stretch(list, dead, arch, next);
         // list scheduling over locations: after every earlier writer of what
         // an operation reads or writes, not before an earlier reader of what
         // it writes
         const size_t b0 = s.ctl.size();
         std::vector<int> count, last_write(next, -1), max_read(next, -1);
-        for (const UOp &u : list) {
+        for (size_t li = 0; li < list.size(); li++) {
+            if (dead[li]) continue;
+            const UOp &u = list[li];
             int earliest = 0;
             for (int k = 0; k < u.nreads; k++) earliest = std::max(earliest, last_write[u.reads[k]] + 1);
             earliest = std::max(earliest, last_write[u.write] + 1);

@@ -14,7 +14,8 @@ constexpr uint64_t BUNDLE_NOP = ~0ull;       // control code 255: never a real i
 // A bundle slot holds a micro-operation over locations (registers 0..31,
 // scratch slots 32.., then values renamed within a stretch):
 //   bits 0-7 opcode, 8-10 rounding, 11-13 operand a/b/c is a constant index,
-//   14 MOVE (dest = a), 16-27 dest, 28-39 a, 40-51 b, 52-63 c.
+//   14 MOVE (dest = a), 15 operand c read with its sign bit flipped (a NEG
+//   folded into the read), 16-27 dest, 28-39 a, 40-51 b, 52-63 c.
 struct BundleSchedule {
     int G = 1;
     uint32_t nb = 0;

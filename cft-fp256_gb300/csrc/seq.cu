@@ -651,6 +651,7 @@ __global__ void __launch_bounds__(32) k_traj_g(const TrajLaunch L)
                             vb[w] = kb ? __ldg(kons + ib * W + w) : LOC(ib, w);
                             vc[w] = kc ? __ldg(kons + ic * W + w) : LOC(ic, w);
                         }
+                        if ((u >> 15) & 1u) vc[W - 1] ^= 0x80000000u;    // a NEG folded into c
                         if (op <= 3) sf::arith_rt<FMT>(op, va, vb, vc, rnd, res, fl);
                         else sf::simple<FMT>(op, va, vb, vc, res, fl);
                         flags |= fl;

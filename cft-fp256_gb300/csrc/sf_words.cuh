@@ -144,56 +144,6 @@ SFD void shr_jam_imad(uint32_t (&x)[N], int s)
     x[0] |= (st != 0u) ? 1u : 0u;
 }
 
-// shr_jam_imad for wide windows whose shifts of half the window or more
-// are rare (binary256's 16-word FMA window: 256 bits or more of alignment
-// arise only from subnormal operands or exponents hundreds apart, yet one
-// such lane makes every lane of its warp run the two widest stages of the
-// select network). Such a lane moves its upper half down (once or twice)
-// on its own, inside a branch only it takes; the remaining stages are the
-// warp-skipped multiply-add network. The same bits as shr_jam.
-template <int N>
-SFD void shr_jam_imad_far(uint32_t (&x)[N], int s)
-{
-    constexpr int H = N / 2;
-    int sc = s <= 0 ? 0 : (s >= 32 * N ? 32 * N : s);
-    uint32_t st = 0u;
-    if (sc >= 32 * H) {                                   // rare: this lane alone
-#pragma unroll
-        for (int r = 0; r < 2; r++) {
-            if (sc >= 32 * H) {
-                uint32_t out = 0u;
-#pragma unroll
-                for (int i = 0; i < H; i++) out |= x[i];
-                st |= out;
-#pragma unroll
-                for (int i = 0; i < N; i++) x[i] = i + H < N ? x[i + H] : 0u;
-                sc -= 32 * H;
-            }
-        }
-    }
-    const int ws = sc >> 5, bs = sc & 31;                 // ws < H now
-    const int need = warp_stages(ws);
-#pragma unroll
-    for (int b = H / 2; b >= 1; b >>= 1) {
-        if (need & b) {
-            const uint32_t t = (uint32_t)(ws & b) / (uint32_t)b;   // 0 or 1
-            const uint32_t nt = t ^ 1u;
-            uint32_t out = 0u;
-#pragma unroll
-            for (int i = 0; i < b; i++) out |= x[i];
-            st |= imul(out, t);
-#pragma unroll
-            for (int i = 0; i < N; i++)
-                x[i] = (i + b < N) ? imad(x[i + b], t, imul(x[i], nt)) : imul(x[i], nt);
-        }
-    }
-    st |= x[0] & ((1u << bs) - 1u);
-#pragma unroll
-    for (int i = 0; i < N - 1; i++) x[i] = __funnelshift_r(x[i], x[i + 1], bs);
-    x[N - 1] >>= bs;
-    x[0] |= (st != 0u) ? 1u : 0u;
-}
-
 // shl with the word moves and the bit shift as multiply-adds: x[i] << bs
 // is the low word of x[i] * 2^bs and x[i-1] >> (32 - bs) its high word.
 template <int N>

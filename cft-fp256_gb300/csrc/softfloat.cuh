@@ -361,8 +361,7 @@ SFD void fma_general(const Unp<FMT> &ua, const Unp<FMT> &ub, const Unp<FMT> &uc,
                 }
             }
         }
-        if constexpr (N >= 16) sfw::shr_jam_imad_far(X, pbig ? -delta : delta);
-        else sfw::shr_jam_imad(X, pbig ? -delta : delta);
+        sfw::shr_jam_imad(X, pbig ? -delta : delta);
         if (!pbig) ew += delta;
         const int s_big = pbig ? sp : sc, s_small = pbig ? sc : sp;
         // Y + X, or Y - X in two's complement, then the magnitude.

@@ -139,7 +139,8 @@ CFT_API void cftg_traj_free(cftg_traj *t);
  * (REPEAT <-> ENDREP bundle). A micro-operation names locations (registers
  * 0..31, scratch slots 32.., renamed values after them): bits 0-7 opcode,
  * 8-10 rounding attribute, 11-13 operand a/b/c is a constant index, 14 MOVE
- * (dest = a), 16-27 dest, 28-39 a, 40-51 b, 52-63 c. The arrays are filled
+ * (dest = a), 15 operand c is read with its sign bit flipped (a NEG folded
+ * into the read), 16-27 dest, 28-39 a, 40-51 b, 52-63 c. The arrays are filled
  * when cap >= *nb; CFT_ERR_UNSUPPORTED for a program outside the scheduled
  * set. */
 CFT_API cft_status cftg_program_schedule(const void *image, size_t bytes, uint32_t G,

@@ -61,6 +61,9 @@ def replay(oracle, sched, fmt, bank, block, reach, W):
                     continue
                 vals = [np.ascontiguousarray(kons[i] if (u >> (11 + k)) & 1 else loc[i])
                         for k, i in enumerate((ia, ib, ic))]
+                if (u >> 15) & 1:                     # a NEG folded into operand c
+                    vals[2] = vals[2].copy()
+                    vals[2][W - 1] ^= np.uint32(0x80000000)
                 assert oracle.L.sfp_compute(fmt, u & 0xFF, (u >> 8) & 7, vals[0].ctypes.data,
                                             vals[1].ctypes.data, vals[2].ctypes.data,
                                             out.ctypes.data, ctypes.byref(fl)) == 0
@@ -185,3 +188,78 @@ def test_schedule_replay_on_mutated_programs(oracle, key, fmt, slots, base, coun
             assert gflags == A.flags_out, (key, G)
             compared += 1
     assert compared >= count, (key, compared)
+
+
+# A stretch that stresses the schedule's two rewrites (a NEG folded into the
+# operand c that reads it; a stretch-end MOVE folded into its value's
+# producer): a NEG whose operand register is overwritten before the
+# operation that reads the NEG; NEGs read as operands a and b (not folded)
+# and as c; a NEG result that is also the stretch's final value of its
+# register; a register read (its value from before the stretch) after the
+# producer of its final value in program order; a value stored to two
+# slots; a slot loaded after a store to another slot.
+HAZARDS = """
+.format   fp64
+.deposits 0
+.scratch  in 3
+.scratch  out 3
+ldl  r1, 0
+ldl  r2, 1
+ldl  r6, 2
+repeat 5
+  neg  r3, r1
+  add  r1, r1, r2
+  fma  r4, r2, r2, r3
+  neg  r5, r4
+  mul  r7, r5, r3
+  fma  r8, r7, r1, r5
+  neg  r9, r8
+  fma  r2, r9, r6, r9
+  sub  r6, r6, r2
+  fma  r10, r6, r2, r6
+  neg  r6, r10
+  stl  r8, 2
+  stl  r8, 0
+  ldl  r11, 1
+  fma  r1, r11, r3, r1
+endrep
+stl  r1, 0
+stl  r2, 1
+halt
+"""
+
+
+@pytest.mark.parametrize("G", [1, 2, 4, 8, 32])
+def test_schedule_rewrites_keep_the_sequencer_s_values(oracle, G):
+    from cftgb import asm
+    oracle.L.sfp_compute.argtypes = [ctypes.c_int] * 3 + [ctypes.c_void_p] * 4 + [
+        ctypes.POINTER(ctypes.c_uint32)]
+    img = np.frombuffer(asm.assemble(HAZARDS, "hazards.cfta"), np.uint8).copy()
+    sched = schedule(img, G)
+    assert sched is not None
+    W = 2
+    rng = np.random.default_rng(G)
+    for trial in range(4):
+        vals = rng.uniform(-2.0, 2.0, size=3)
+        init = np.array([wl.from_int(wl.encode_double(1, float(v)), W) for v in vals], np.uint32)
+        got, gflags = replay(oracle, sched, 1, None, init, 256, W)
+        out = np.zeros_like(init)
+        A = oracle_lib.SeqArgs()
+        a = np.zeros((1, W), np.uint32)
+        A.a, A.n = a.ctypes.data, 1
+        A.scratch_in, A.scratch_out, A.depth = init.ctypes.data, out.ctypes.data, 256
+        assert oracle.L.sfp_seq_run(img.ctypes.data, img.size, ctypes.byref(A)) == 0
+        assert np.array_equal(got[:3], out), (G, trial)
+        assert gflags == A.flags_out
+
+
+def test_schedule_rewrites_fold_the_ode_negations():
+    """Lorenz-63's step: the NEGs leave the chains that read them and the
+    stretch's end MOVEs are gone, so at 8 threads a lane a step is at most
+    18 bundles (25 without the rewrites); no micro-operation keeps a NEG of
+    a value only a folded read used."""
+    z = np.load(su.GOLD / "odes.npz")
+    ops, ctl, _, _ = schedule(z["l63_image"].copy(), 8)
+    assert len(ctl) <= 18, len(ctl)
+    words = [int(u) for u in ops.reshape(-1) if int(u) != NOP]
+    assert any((u >> 15) & 1 for u in words)
