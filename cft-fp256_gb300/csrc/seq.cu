@@ -579,7 +579,7 @@ __global__ void k_traj(const TrajLaunch L, bool scratch_shared)
 // regions or raises are scheduled, so the lane byte holds the IEEE flags
 // alone and STATUS stays 0.
 template <int FMT, bool EARLY>
-__global__ void __launch_bounds__(32) k_traj_g(const TrajLaunch L)
+__global__ void __launch_bounds__(32) k_traj_g(const TrajLaunch L, uint32_t staged)
 {
     constexpr int W = sf::Fmt<FMT>::W;
     extern __shared__ uint32_t smem[];
@@ -597,6 +597,32 @@ __global__ void __launch_bounds__(32) k_traj_g(const TrajLaunch L)
     uint32_t *state = static_cast<uint32_t *>(L.state);
     uint32_t *snaps = static_cast<uint32_t *>(L.snaps);
     const uint32_t *kons = static_cast<const uint32_t *>(P.d_consts);
+    const uint64_t *b_ops = L.b_ops;
+    const uint32_t *b_ctl = L.b_ctl, *b_arg = L.b_arg;
+    const int32_t *b_match = L.b_match;
+    // the schedule and the constants, read at every bundle, into shared
+    // memory after the lane's locations (word offset `staged`; 0: left in
+    // global memory)
+    if (staged) {
+        const uint32_t nb = L.nb, nops = nb * (uint32_t)G;
+        uint64_t *so = reinterpret_cast<uint64_t *>(smem + staged);
+        uint32_t *sw = reinterpret_cast<uint32_t *>(so + nops);
+        for (uint32_t i = t; i < nops; i += 32) so[i] = L.b_ops[i];
+        for (uint32_t i = t; i < nb; i += 32) {
+            sw[i] = L.b_ctl[i];
+            sw[nb + i] = L.b_arg[i];
+            sw[2 * nb + i] = (uint32_t)L.b_match[i];
+        }
+        uint32_t *sk = sw + 3 * nb;
+        if (kons)
+            for (uint32_t i = t; i < P.n_consts * (uint32_t)W; i += 32) sk[i] = kons[i];
+        __syncwarp();
+        b_ops = so;
+        b_ctl = sw;
+        b_arg = sw + nb;
+        b_match = reinterpret_cast<const int32_t *>(sw + 2 * nb);
+        if (kons) kons = sk;
+    }
     if (have) {
         for (uint32_t sl = g; sl < slots; sl += G) {
 #pragma unroll
@@ -630,9 +656,9 @@ __global__ void __launch_bounds__(32) k_traj_g(const TrajLaunch L)
         int sp = 0;
         uint32_t b = 0;
         while (b < L.nb) {
-            const uint32_t kind = __ldg(L.b_ctl + b);
+            const uint32_t kind = b_ctl[b];
             if (kind == 0u) {                              // micro-operations
-                const uint64_t u = __ldg(L.b_ops + (size_t)b * G + g);
+                const uint64_t u = b_ops[(size_t)b * G + g];
                 uint32_t res[W];
                 int dest = -1;
                 if (mine && u != ~0ull) {
@@ -647,9 +673,9 @@ __global__ void __launch_bounds__(32) k_traj_g(const TrajLaunch L)
                         uint32_t va[W], vb[W], vc[W], fl = 0u;
 #pragma unroll
                         for (int w = 0; w < W; w++) {
-                            va[w] = ka ? __ldg(kons + ia * W + w) : LOC(ia, w);
-                            vb[w] = kb ? __ldg(kons + ib * W + w) : LOC(ib, w);
-                            vc[w] = kc ? __ldg(kons + ic * W + w) : LOC(ic, w);
+                            va[w] = ka ? kons[ia * W + w] : LOC(ia, w);
+                            vb[w] = kb ? kons[ib * W + w] : LOC(ib, w);
+                            vc[w] = kc ? kons[ic * W + w] : LOC(ic, w);
                         }
                         if ((u >> 15) & 1u) vc[W - 1] ^= 0x80000000u;    // a NEG folded into c
                         if (op <= 3) sf::arith_rt<FMT>(op, va, vb, vc, rnd, res, fl);
@@ -667,9 +693,9 @@ __global__ void __launch_bounds__(32) k_traj_g(const TrajLaunch L)
                 b++;
             } else if (kind == 1u) {                       // REPEAT
                 const bool any = __any_sync(0xFFFFFFFFu, mine);
-                const uint32_t imm = __ldg(L.b_arg + b);
+                const uint32_t imm = b_arg[b];
                 if (imm == 0u || !any) {
-                    b = (uint32_t)__ldg(L.b_match + b) + 1u;
+                    b = (uint32_t)b_match[b] + 1u;
                 } else if (sp >= 4) {
                     err |= 1u;
                     break;
@@ -852,20 +878,29 @@ static cudaError_t go_traj_g(const TrajLaunch &L, cudaStream_t s)
 {
     constexpr int W = sf::Fmt<FMT>::W;
     const int LPB = 32 / L.G;
-    const size_t need = (size_t)L.nloc * (size_t)(W * LPB + 1) * 4;
+    size_t need = (size_t)L.nloc * (size_t)(W * LPB + 1) * 4;
+    // the schedule and the constant bank after the locations, 8-byte
+    // aligned, when the block's shared memory stays within 96 KB with them
+    const size_t at = (need + 7) / 8 * 8;
+    const size_t extra = (size_t)L.nb * L.G * 8 + (size_t)L.nb * 12 + (size_t)L.P.n_consts * W * 4;
+    uint32_t staged = 0;
+    if (at + extra <= (96u << 10)) {
+        staged = (uint32_t)(at / 4);
+        need = at + extra;
+    }
     const size_t blocks = (L.n + LPB - 1) / LPB;
     if (L.req_of) {
         const size_t smem = capped_smem(k_traj_g<FMT, true>, L, 32, need);
         static unsigned done = 0;
         cudaError_t e = smem_ceiling_once(k_traj_g<FMT, true>, done);
         if (e != cudaSuccess) return e;
-        k_traj_g<FMT, true><<<(unsigned)blocks, 32, smem, s>>>(L);
+        k_traj_g<FMT, true><<<(unsigned)blocks, 32, smem, s>>>(L, staged);
     } else {
         const size_t smem = capped_smem(k_traj_g<FMT, false>, L, 32, need);
         static unsigned done = 0;
         cudaError_t e = smem_ceiling_once(k_traj_g<FMT, false>, done);
         if (e != cudaSuccess) return e;
-        k_traj_g<FMT, false><<<(unsigned)blocks, 32, smem, s>>>(L);
+        k_traj_g<FMT, false><<<(unsigned)blocks, 32, smem, s>>>(L, staged);
     }
     return cudaGetLastError();
 }
