@@ -86,3 +86,76 @@ def _queue_matches_plain(gpu, L):
         assert torch.equal(outs_plain[i], outs_q[i]), i
     assert torch.equal(torch.cat(plain_flags), flags)
     L.cftg_batch_free(b)
+
+
+KINDS5 = [(0, 1, "add"), (0, 3, "mul"), (0, 0, "fma"), (1, 0, "div"), (2, 0, "sqrt")]
+
+
+@pytest.mark.parametrize("threads", [256, 128])
+def test_queue_matches_oracle(gpu, oracle, threads):
+    """The batched form against the oracle itself, not only against the
+    plain kernels (which share its element code): binary64/128/256 x add,
+    mul, fma, div, sqrt x all five attributes, sizes across tile edges
+    (1 to 4,097 elements) and three calls of 2^20 (the uneven batch's
+    largest), every element's value and every call's flag word, as one
+    launch and again replayed from a CUDA graph, at both block shapes."""
+    import torch
+    L = cftgb.lib()
+    vp = ctypes.c_void_p
+    L.cftg_batch_create.argtypes = [vp, ctypes.POINTER(Call), ctypes.c_size_t, vp, ctypes.POINTER(vp)]
+    L.cftg_batch_launch.argtypes = [vp, vp]
+    L.cftg_batch_capture.argtypes = [vp, vp]
+    L.cftg_batch_free.argtypes = [vp]
+    before = L.cftg_queue_block_threads()
+    cftgb._lib.check(L.cftg_set_queue_block_threads(threads), "cftg_set_queue_block_threads")
+    try:
+        rng = np.random.default_rng(77)
+        edges = [1, 2, 31, 255, 256, 257, 1023, 1025, 4097]
+        spec = []
+        for fmt in (1, 2, 3):
+            for kind, op, _ in KINDS5:
+                for rnd in range(5):
+                    spec.append((fmt, kind, op, rnd, edges[int(rng.integers(0, len(edges)))]))
+        spec += [(1, 1, 0, 2, 1 << 20), (2, 2, 0, 4, 1 << 20), (3, 0, 0, 0, 1 << 20)]
+        calls = (Call * len(spec))()
+        keep, host, outs = [], [], []
+        for i, (fmt, kind, op, rnd, n) in enumerate(spec):
+            a, b, c = wl.gen_operands(fmt, n, 5000 + i, ties=n >= 4)
+            ta, tb, tc = (torch.from_numpy(x.view(np.int32)).cuda() for x in (a, b, c))
+            td = torch.zeros_like(ta)
+            calls[i] = Call(kind, op, fmt, rnd, ta.data_ptr(), tb.data_ptr(), tc.data_ptr(),
+                            td.data_ptr(), n, 0)
+            keep += [ta, tb, tc]
+            host.append((a, b, c))
+            outs.append(td)
+        want = [oracle.run_parallel(kind, fmt, op, rnd, *host[i])
+                for i, (fmt, kind, op, rnd, n) in enumerate(spec)]
+        flags = torch.zeros(len(spec), dtype=torch.int32, device="cuda")
+        bt = ctypes.c_void_p()
+        cftgb._lib.check(L.cftg_batch_create(gpu, calls, len(spec), flags.data_ptr(), ctypes.byref(bt)),
+                         "create")
+        stream = torch.cuda.current_stream().cuda_stream
+
+        def check(where):
+            got_flags = flags.cpu().numpy().view(np.uint32)
+            for i, (fmt, kind, op, rnd, n) in enumerate(spec):
+                d = outs[i].cpu().numpy().view(np.uint32).reshape(n, -1)
+                rd, _, racc = want[i]
+                bad = np.nonzero((d != rd).any(1))[0]
+                assert bad.size == 0, (where, fmt, kind, op, rnd, n, bad[:4])
+                assert int(got_flags[i]) & 0x1F == racc, (where, fmt, kind, op, rnd, n)
+
+        cftgb._lib.check(L.cftg_batch_launch(bt, stream), "launch")
+        torch.cuda.synchronize()
+        check("launch")
+        s2 = torch.cuda.Stream()
+        for o in outs:
+            o.zero_()
+        flags.zero_()
+        cftgb._lib.check(L.cftg_batch_capture(bt, s2.cuda_stream), "capture")
+        cftgb._lib.check(L.cftg_batch_launch(bt, s2.cuda_stream), "replay")
+        s2.synchronize()
+        check("graph replay")
+        L.cftg_batch_free(bt)
+    finally:
+        cftgb._lib.check(L.cftg_set_queue_block_threads(before), "cftg_set_queue_block_threads")
