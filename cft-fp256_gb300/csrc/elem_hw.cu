@@ -23,8 +23,9 @@
 //  * an infinite r from finite operands: an overflow rounded to the
 //    infinity, as the reference rounds it, with OVERFLOW and INEXACT (a
 //    largest-magnitude r may or may not be an overflow, so it is not taken);
-//  * a NaN or an infinity among the operands: the reference's special cases
-//    straight from the encodings (hw_special).
+//  * a NaN or an infinity among the operands: IEEE 754's NaN or infinity is
+//    the reference's special case in value (the NaN made the canonical
+//    quiet NaN), with INVALID worked out from the operands' encodings.
 // What remains - subnormal and tiny results, and largest-magnitude ones -
 // takes the integer path.
 //
@@ -52,7 +53,7 @@ namespace cftg {
 namespace {
 
 constexpr uint32_t EXP32 = 0x7F800000u, MAG_MAX32 = 0x7F7FFFFFu, QNAN32 = 0x7FC00000u;
-constexpr uint32_t ONE32 = 0x3F800000u, SIGN32 = 0x80000000u;
+constexpr uint32_t SIGN32 = 0x80000000u;
 
 // The operation in one direction (ADD/SUB read a and c, MUL a and b).
 template <int KIND, int DIR>
@@ -81,8 +82,24 @@ SFD float hw_op(float a, float b, float c)
     }
 }
 
-// One element on the hardware: the encoding in o, INEXACT in fl, and
-// whether the element qualifies (see the rules above).
+SFD bool nan32(uint32_t u) { return (u & ~SIGN32) > EXP32; }
+SFD bool inf32(uint32_t u) { return (u & ~SIGN32) == EXP32; }
+SFD bool snan32(uint32_t u) { return nan32(u) && !(u & (1u << 22)); }
+
+// One element on the hardware: the encoding in o and the flags in fl, and
+// whether the element is finished (false: it is for the integer path).
+// Branch-free; the outcomes (see the rules above):
+//  * a NaN result: the canonical quiet NaN; INVALID iff an operand the kind
+//    reads is a signalling NaN, or no operand is a NaN (inf * 0, inf - inf);
+//  * an infinite result: exact when an operand is infinite, else an
+//    overflow (OVERFLOW, INEXACT);
+//  * a normal result of biased exponent >= 2 that is not the largest
+//    magnitude, or an exact zero: INEXACT = (RD(x) != RU(x)).
+// IEEE 754's results for NaN and infinite operands are the reference's
+// special cases (host/src/softfloat.c:335-373) in value, the NaN's
+// encoding aside: inf * 0 and inf - inf give a NaN, an infinite product or
+// addend gives the infinity of its sign, under the steering ADD/SUB =
+// a*1 + (+-c) and MUL = a*b + (+-0).
 template <int KIND, int RND>
 SFD bool hw_elem(uint32_t a, uint32_t b, uint32_t c, uint32_t &o, uint32_t &fl)
 {
@@ -93,50 +110,22 @@ SFD bool hw_elem(uint32_t a, uint32_t b, uint32_t c, uint32_t &o, uint32_t &fl)
     if constexpr (RND == sf::RNE) r = hw_op<KIND, sf::RNE>(fa, fb, fc);
     else if constexpr (RND == sf::RDN) r = lo;
     else if constexpr (RND == sf::RUP) r = hi;
-    else r = lo > 0.0f ? lo : hi;                   // RTZ: toward zero (the result is not 0)
-    o = __float_as_uint(r);
-    fl = lo != hi ? sf::F_INEXACT : 0u;
-    const uint32_t e = o & EXP32, mag = o & ~SIGN32;
+    else r = lo > 0.0f ? lo : hi;                   // RTZ: toward zero
+    const uint32_t u = __float_as_uint(r);
+    const uint32_t e = u & EXP32, mag = u & ~SIGN32;
+    const bool rb = KIND == K_FMA || KIND == K_MUL, rc = KIND != K_MUL;
+    const bool any_nan = nan32(a) || (rb && nan32(b)) || (rc && nan32(c));
+    const bool any_snan = snan32(a) || (rb && snan32(b)) || (rc && snan32(c));
+    const bool any_inf = inf32(a) || (rb && inf32(b)) || (rc && inf32(c));
+    const bool r_nan = mag > EXP32, r_inf = mag == EXP32;
+    const uint32_t inexact = lo != hi ? sf::F_INEXACT : 0u;
+    o = r_nan ? QNAN32 : u;
+    fl = r_nan ? ((any_snan || !any_nan) ? sf::F_INVALID : 0u)
+               : r_inf ? (any_inf ? 0u : sf::F_OVERFLOW | sf::F_INEXACT) : inexact;
     // an exact zero (RD and RU agree, so the exact value is 0): IEEE 754's
     // signs of an exact zero sum are the reference's (+0, or -0 under RDN,
     // when the signs differ; the common sign otherwise)
-    return (e >= (2u << 23) && e != EXP32 && mag != MAG_MAX32) || (mag == 0u && lo == hi);
-}
-
-SFD bool nan32(uint32_t u) { return (u & ~SIGN32) > EXP32; }
-SFD bool inf32(uint32_t u) { return (u & ~SIGN32) == EXP32; }
-
-// An element with a NaN or an infinity among its steered operands: the
-// reference's special cases in its order (host/src/softfloat.c:335-373),
-// ADD/SUB steered to a*1 + (+-c), MUL to a*b + (+-0). Returns false when
-// no operand is a NaN or an infinity (the element is for the integer path).
-template <int KIND>
-SFD bool hw_special(uint32_t a, uint32_t b, uint32_t c, uint32_t &o, uint32_t &fl)
-{
-    const uint32_t ub = (KIND == K_ADD || KIND == K_SUB) ? ONE32 : b;
-    uint32_t uc = KIND == K_MUL ? ((a ^ ub) & SIGN32) : c;
-    if constexpr (KIND == K_SUB) uc ^= SIGN32;
-    const bool na = nan32(a), nb = nan32(ub), nc = nan32(uc);
-    const bool ia = inf32(a), ib = inf32(ub), ic = inf32(uc);
-    if (!(na || nb || nc || ia || ib || ic)) return false;
-    const uint32_t sp = (a ^ ub) & SIGN32;
-    fl = 0u;
-    if (na || nb || nc) {
-        o = QNAN32;
-        const uint32_t quiet = 1u << 22;
-        fl = ((na && !(a & quiet)) || (nb && !(ub & quiet)) || (nc && !(uc & quiet))) ? sf::F_INVALID
-                                                                                       : 0u;
-    } else if (ia || ib) {
-        if ((a & ~SIGN32) == 0u || (ub & ~SIGN32) == 0u || (ic && (uc & SIGN32) != sp)) {
-            o = QNAN32;                                // inf * 0, inf - inf
-            fl = sf::F_INVALID;
-        } else {
-            o = sp | EXP32;
-        }
-    } else {
-        o = uc;                                        // c is the infinity
-    }
-    return true;
+    return r_nan || r_inf || (e >= (2u << 23) && mag != MAG_MAX32) || (mag == 0u && lo == hi);
 }
 
 // The integer path for one queued element (one copy of its code a kernel).
@@ -227,17 +216,7 @@ __global__ void __launch_bounds__(HW_T, 4) k_elem_hw(const __grid_constant__ Ele
             const uint32_t off = (uint32_t)(k * HW_T + tid);
             const size_t i = base + off;
             uint32_t o, fl;
-            bool ok = hw_elem<KIND, RND>(a[k], b[k], c[k], o, fl);
-            if (!ok) {
-                ok = hw_special<KIND>(a[k], b[k], c[k], o, fl);
-                // finite operands and an infinite result: an overflow, whose
-                // rounding (up to the infinity) the hardware did as the
-                // reference does; OVERFLOW and INEXACT
-                if (!ok && (o & ~SIGN32) == EXP32) {
-                    fl = sf::F_OVERFLOW | sf::F_INEXACT;
-                    ok = true;
-                }
-            }
+            const bool ok = hw_elem<KIND, RND>(a[k], b[k], c[k], o, fl);
             const bool in = off < left;
             if (in && ok) {
                 pd[i] = o;
