@@ -678,7 +678,8 @@ __global__ void __launch_bounds__(32) k_traj_g(const TrajLaunch L, uint32_t stag
                             vc[w] = kc ? kons[ic * W + w] : LOC(ic, w);
                         }
                         if ((u >> 15) & 1u) vc[W - 1] ^= 0x80000000u;    // a NEG folded into c
-                        if (op <= 3) sf::arith_rt<FMT>(op, va, vb, vc, rnd, res, fl);
+                        // latency form: this warp's lanes wait on each result
+                        if (op <= 3) sf::arith_rt<FMT, true>(op, va, vb, vc, rnd, res, fl);
                         else sf::simple<FMT>(op, va, vb, vc, res, fl);
                         flags |= fl;
                     }

@@ -190,8 +190,9 @@ SFD void take_top(const uint32_t (&m)[N], uint32_t (&kept)[Fmt<FMT>::W], bool &g
 // carry a jammed sticky, which must sit at least two places below the
 // rounding point) into the format. Writes the encoding and the flags.
 // ZERO: m may be zero (an exact cancellation), which gives +0, or -0 under
-// roundTowardNegative, with no flag.
-template <int FMT, int N, bool ZERO = false>
+// roundTowardNegative, with no flag. LAT: the form for a lone warp waiting
+// on one result (shifts as selects on the integer ALU; see fma_general).
+template <int FMT, int N, bool ZERO = false, bool LAT = false>
 SFD void round_pack(int sign, uint32_t (&m)[N], int e, int rnd, uint32_t (&out)[Fmt<FMT>::W],
                     uint32_t &flags)
 {
@@ -217,7 +218,7 @@ SFD void round_pack(int sign, uint32_t (&m)[N], int e, int rnd, uint32_t (&out)[
     const int e_norm = e + L - 1;                 // exponent of the leading bit
     // leading bit to the top; narrow windows shift on the IMAD pipe, wide
     // ones (whose products already load it) on the integer ALU
-    if constexpr (N <= 5) sfw::shl_imad(m, 32 * N - L);
+    if constexpr (N <= 5 && !LAT) sfw::shl_imad(m, 32 * N - L);
     else sfw::shl(m, 32 * N - L);
 
     uint32_t kept[W];
@@ -310,7 +311,16 @@ enum { OP_FMA = 0, OP_ADD = 1, OP_SUB = 2, OP_MUL = 3 };
 // (operands' true low bits are zero there, so subtracting a jammed operand
 // leaves bit 0 set). Rounding at any position >= 2 then reads the right
 // kept bits, guard and sticky.
-template <int FMT, int OP>
+//
+// LAT selects the form for a warp that waits on this one result (a
+// trajectory's dependent chain on a lightly loaded scheduler) rather than
+// for many warps sharing the integer pipes: the product as two independent
+// chains of carry chains (mul_ptx_split), and the selects, the alignment
+// shift and the complement as selects and XORs on the integer ALU pipe
+// (one instruction a word) instead of multiply-adds (two a word on the
+// IMAD pipe, which balance the pipes under load but lengthen a lone
+// chain). The same bits either way.
+template <int FMT, int OP, bool LAT = false>
 SFD void fma_general(const Unp<FMT> &ua, const Unp<FMT> &ub, const Unp<FMT> &uc, int sc, int rnd,
                      uint32_t (&out)[Fmt<FMT>::W], uint32_t &flags)
 {
@@ -329,7 +339,8 @@ SFD void fma_general(const Unp<FMT> &ua, const Unp<FMT> &ub, const Unp<FMT> &uc,
         sfw::shr_const<1>(P);                              // leading bit at 64W-3
         ew = ua.ve - (64 * W - 3);
     } else {
-        sfw::mul_ptx<W>(P, ua.m, ub.m);
+        if constexpr (LAT) sfw::mul_ptx_split<W>(P, ua.m, ub.m);
+        else sfw::mul_ptx<W>(P, ua.m, ub.m);
         ew = ua.ve + ub.ve - (64 * W - 3);
     }
 
@@ -347,8 +358,14 @@ SFD void fma_general(const Unp<FMT> &ua, const Unp<FMT> &ub, const Unp<FMT> &uc,
         const int delta = czero ? -(1 << 28) : uc.ve - (ew + 64 * W - 2);
         const bool pbig = delta <= 0;
         uint32_t X[N], Y[N];
-        // the selections as multiply-adds by 0 and 1 (IMAD pipe)
-        {
+        if constexpr (LAT) {
+#pragma unroll
+            for (int i = 0; i < N; i++) {
+                X[i] = pbig ? C[i] : P[i];
+                Y[i] = pbig ? P[i] : C[i];
+            }
+        } else {
+            // the selections as multiply-adds by 0 and 1 (IMAD pipe)
             const uint32_t pb = pbig ? 1u : 0u, npb = pb ^ 1u;
 #pragma unroll
             for (int i = 0; i < N; i++) {
@@ -361,7 +378,8 @@ SFD void fma_general(const Unp<FMT> &ua, const Unp<FMT> &ub, const Unp<FMT> &uc,
                 }
             }
         }
-        sfw::shr_jam_imad(X, pbig ? -delta : delta);
+        if constexpr (LAT) sfw::shr_jam(X, pbig ? -delta : delta);
+        else sfw::shr_jam_imad(X, pbig ? -delta : delta);
         if (!pbig) ew += delta;
         const int s_big = pbig ? sp : sc, s_small = pbig ? sc : sp;
         // Y + X, or Y - X in two's complement, then the magnitude.
@@ -372,7 +390,7 @@ SFD void fma_general(const Unp<FMT> &ua, const Unp<FMT> &ub, const Unp<FMT> &uc,
 #pragma unroll
         for (int i = 0; i < N; i++) {
             P[i] = Y[i];
-            X[i] = sfw::imad(X[i], m1, mk);
+            X[i] = LAT ? X[i] ^ mk : sfw::imad(X[i], m1, mk);
         }
         const uint32_t cy = sfw::AddPtx<N>::add(P, X, sub ? 1u : 0u);
         const bool neg = sub && !cy;               // Y < X: the result is X - Y
@@ -393,7 +411,7 @@ SFD void fma_general(const Unp<FMT> &ua, const Unp<FMT> &ub, const Unp<FMT> &uc,
     }
     // an exact cancellation (only an effective subtraction gives one) leaves
     // P zero, which round_pack answers with the zero of the attribute
-    round_pack<FMT, N, OP != OP_MUL>(rs, P, ew, rnd, out, flags);
+    round_pack<FMT, N, OP != OP_MUL, LAT>(rs, P, ew, rnd, out, flags);
 }
 
 // The steered operands of FMA/ADD/SUB/MUL, unpacked: x/y/z are the
@@ -465,17 +483,59 @@ SFD bool arith_special_case(const Unp<FMT> &ua, const Unp<FMT> &ub, const Unp<FM
     return false;
 }
 
+// unpack for an operand known to be normal (unpack's last case alone)
+template <int FMT, int LB>
+SFD void unpack_normal(const uint32_t (&x)[Fmt<FMT>::W], Unp<FMT> &u)
+{
+    using F = Fmt<FMT>;
+    constexpr int W = F::W;
+    u.sign = sign_of<FMT>(x);
+    u.snan = 0;
+    u.cls = C_NORM;
+    u.ve = (int)exp_field<FMT>(x) - F::BIAS;
+#pragma unroll
+    for (int i = 0; i < W; i++) u.m[i] = x[i];
+    u.m[W - 1] = (u.m[W - 1] & ((1u << exp_shift<FMT>()) - 1u)) | (1u << exp_shift<FMT>());
+    sfw::shl_const<LB - F::MANW>(u.m);
+}
+
 // One element of FMA/ADD/SUB/MUL: the special cases, else the general path.
-template <int FMT, int OP>
+// LAT (a lone warp waiting on the result, fma_general): the usual operands -
+// a and b normal, c normal or zero, which take no special case - are told
+// apart by one test and unpacked without unpack's class branches.
+template <int FMT, int OP, bool LAT = false>
 SFD void arith(const uint32_t (&x)[Fmt<FMT>::W], const uint32_t (&y)[Fmt<FMT>::W],
                const uint32_t (&z)[Fmt<FMT>::W], int rnd, uint32_t (&out)[Fmt<FMT>::W],
                uint32_t &flags)
 {
+    constexpr int W = Fmt<FMT>::W;
+    if constexpr (LAT && OP == OP_FMA) {
+        constexpr uint32_t EM = exp_mask<FMT>();
+        uint32_t zm = z[W - 1] & 0x7FFFFFFFu;
+#pragma unroll
+        for (int i = 0; i < W - 1; i++) zm |= z[i];
+        const bool cz = zm == 0u;
+        const uint32_t ea = exp_field<FMT>(x), eb = exp_field<FMT>(y), ec = exp_field<FMT>(z);
+        if ((ea - 1u) < EM - 1u && (eb - 1u) < EM - 1u && ((ec - 1u) < EM - 1u || cz)) {
+            Unp<FMT> ua, ub, uc;
+            unpack_normal<FMT, 32 * W - 2>(x, ua);
+            unpack_normal<FMT, 32 * W - 1>(y, ub);
+            unpack_normal<FMT, 32 * W - 2>(z, uc);
+            if (cz) {
+                uc.cls = C_ZERO;
+                uc.ve = 0;
+#pragma unroll
+                for (int i = 0; i < W; i++) uc.m[i] = 0u;
+            }
+            fma_general<FMT, OP, true>(ua, ub, uc, uc.sign, rnd, out, flags);
+            return;
+        }
+    }
     Unp<FMT> ua, ub, uc;
     uint32_t csteer[Fmt<FMT>::W];
     steer_unpack<FMT, OP>(x, y, z, ua, ub, uc, csteer);
     if (arith_special_case<FMT>(ua, ub, uc, csteer, rnd, out, flags)) return;
-    fma_general<FMT, OP>(ua, ub, uc, uc.sign, rnd, out, flags);
+    fma_general<FMT, OP, LAT>(ua, ub, uc, uc.sign, rnd, out, flags);
 }
 
 // FMA/ADD/SUB/MUL with the operation chosen at run time, all through the one
@@ -484,8 +544,8 @@ SFD void arith(const uint32_t (&x)[Fmt<FMT>::W], const uint32_t (&y)[Fmt<FMT>::W
 // steering; the special cases then see the steered operands. One copy of
 // the code serves every arithmetic opcode, which keeps an interpreter's
 // instruction footprint small and lets threads that run different opcodes
-// of this family stay converged.
-template <int FMT>
+// of this family stay converged. LAT: see arith.
+template <int FMT, bool LAT = false>
 SFD void arith_rt(int op, const uint32_t (&x)[Fmt<FMT>::W], const uint32_t (&y)[Fmt<FMT>::W],
                   const uint32_t (&z)[Fmt<FMT>::W], int rnd, uint32_t (&out)[Fmt<FMT>::W],
                   uint32_t &flags)
@@ -503,7 +563,7 @@ SFD void arith_rt(int op, const uint32_t (&x)[Fmt<FMT>::W], const uint32_t (&y)[
     if (addsub) b[W - 1] = (uint32_t)F::BIAS << ES;                       // +1
     if (op == OP_SUB) c[W - 1] ^= 0x80000000u;
     if (op == OP_MUL) c[W - 1] = (x[W - 1] ^ y[W - 1]) & 0x80000000u;    // +-0
-    arith<FMT, OP_FMA>(x, b, c, rnd, out, flags);
+    arith<FMT, OP_FMA, LAT>(x, b, c, rnd, out, flags);
 }
 
 // ---- exact division of significands ---------------------------------------
