@@ -422,13 +422,21 @@ namespace cftg {
 // then share a scheduler (152 SMs x 4), with a bundle counted a quarter
 // dearer than one instruction of the plain interpreter (two warp barriers,
 // operands read from shared memory). G = 1 keeps the plain interpreter.
+// Binary128/256 programs may also take the cooperative arithmetic
+// (coop.cuh): W threads a micro-operation, so G threads hold G/W of them a
+// bundle, a bundle counted at COOP_BUNDLE instead; only when
+// CFTG_LANE_COOP=1 asks for it (see below). CFTG_LANE_THREADS forces G.
 void plan_lanes(cft_program *prog, size_t n, TrajLaunch &L)
 {
+    constexpr double PLAIN_BUNDLE = 1.25, COOP_BUNDLE = 0.8;
     L.G = 1;
+    L.K = 1;
     L.nb = 0;
     if (!prog || !n) return;
     const char *env = getenv("CFTG_LANE_THREADS");
-    int forced = env ? atoi(env) : 0;
+    const int forced = env ? atoi(env) : 0;
+    const char *cenv = getenv("CFTG_LANE_COOP");
+    const int coop_mode = cenv ? atoi(cenv) : 0;
     const double slots = (double)sm_count() * 4.0;
     auto contention = [&](int G) {
         const double warps = std::ceil((double)n * G / 32.0);
@@ -438,20 +446,31 @@ void plan_lanes(cft_program *prog, size_t n, TrajLaunch &L)
     if (!one) return;                                  // not schedulable: plain interpreter
     const int W = (int)(esz_of(L.P.fmt) / 4);
     double best = one->ops_weighted * contention(1);
-    int bestG = 1;
-    for (int G = 2; G <= 32; G *= 2) {
-        if (forced && G != forced) continue;
-        const DevBundles *d = program_bundles(prog, G);
-        if (!d || (size_t)d->nloc * (size_t)(W * (32 / G) + 1) * 4 > (200u << 10)) continue;
-        const double est = d->weighted * 1.25 * contention(G);
-        if (forced || est < best) {
+    int bestG = 1, bestK = 1;
+    // a forced G takes its first candidate, and the cooperative one instead
+    // only when it is estimated cheaper (or forced too)
+    auto consider = [&](int G, int K, double cost) {
+        const DevBundles *d = program_bundles(prog, G / K);
+        if (!d) return;
+        size_t bytes = (size_t)d->nloc * (size_t)(W * (32 / G) + 1) * 4;
+        if (K > 1) bytes += (size_t)(32 / W) * (size_t)(9 * W) * 4;
+        if (bytes > (200u << 10)) return;
+        const double est = d->weighted * cost * contention(G);
+        if ((forced && bestG != G) || est < best) {
             best = est;
             bestG = G;
+            bestK = K;
         }
+    };
+    for (int G = 2; G <= 32; G *= 2) {
+        if (forced && G != forced) continue;
+        if (coop_mode != 1 || W < 4) consider(G, 1, PLAIN_BUNDLE);
+        if (coop_mode == 1 && W >= 4 && G >= W) consider(G, W, COOP_BUNDLE);
     }
     if (bestG == 1) return;
-    const DevBundles *d = program_bundles(prog, bestG);
+    const DevBundles *d = program_bundles(prog, bestG / bestK);
     L.G = bestG;
+    L.K = bestK;
     L.nb = d->nb;
     L.nloc = d->nloc;
     L.b_ops = d->ops;

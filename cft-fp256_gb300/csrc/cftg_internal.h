@@ -139,8 +139,11 @@ struct TrajLaunch {
     uint32_t *lane_status = nullptr;   // n words: each lane's STATUS, or NULL
     uint32_t *word = nullptr;     // [0] flags, [1] status, [2] error
     // G > 1: each lane served by G threads through a bundle schedule
-    // (bundle.cpp); G == 1: one thread a lane, the plain interpreter
-    int G = 1;
+    // (bundle.cpp); G == 1: one thread a lane, the plain interpreter. K:
+    // threads a micro-operation (1, or the element's words for the
+    // cooperative binary128/256 arithmetic of coop.cuh), so a bundle holds
+    // G / K micro-operations
+    int G = 1, K = 1;
     uint32_t nb = 0, nloc = 0;                // bundles; a lane's locations
     const uint64_t *b_ops = nullptr;
     const uint32_t *b_ctl = nullptr, *b_arg = nullptr;

@@ -19,6 +19,7 @@
 // the same structure-of-words layout across the launch's lanes.
 #include "aug.cuh"
 #include "cftg_internal.h"
+#include "coop.cuh"
 #include "simple_ops.cuh"
 
 namespace cftg {
@@ -578,14 +579,22 @@ __global__ void k_traj(const TrajLaunch L, bool scratch_shared)
 // programs without deposits, lane-mask changes, indexed scratch, quiet
 // regions or raises are scheduled, so the lane byte holds the IEEE flags
 // alone and STATUS stays 0.
-template <int FMT, bool EARLY>
-__global__ void __launch_bounds__(32) k_traj_g(const TrajLaunch L, uint32_t staged)
+//
+// COOP (binary128/256): each micro-operation is computed by a group of W
+// threads (coop.cuh), thread j of it writing word j of the result; a lane's
+// G threads then hold G/W micro-operations a bundle, and the group's scratch
+// sits in shared memory at word coop_at.
+template <int FMT, bool EARLY, bool COOP>
+__global__ void __launch_bounds__(32) k_traj_g(const TrajLaunch L, uint32_t staged,
+                                               uint32_t coop_at)
 {
     constexpr int W = sf::Fmt<FMT>::W;
+    constexpr int K = COOP ? W : 1;                  // threads a micro-operation
     extern __shared__ uint32_t smem[];
     const SeqProgram &P = L.P;
-    const int G = L.G, LPB = 32 / G;
+    const int G = L.G, LPB = 32 / G, S = G / K;      // S: micro-operations a bundle
     const int t = threadIdx.x, g = t & (G - 1), li = t / G;
+    const int slot = g / K, jw = g & (K - 1);
     const size_t local = (size_t)blockIdx.x * LPB + li;
     const bool have = local < L.n;
     const size_t lane = have ? (L.order ? L.order[local] : local) : 0;
@@ -604,7 +613,7 @@ __global__ void __launch_bounds__(32) k_traj_g(const TrajLaunch L, uint32_t stag
     // memory after the lane's locations (word offset `staged`; 0: left in
     // global memory)
     if (staged) {
-        const uint32_t nb = L.nb, nops = nb * (uint32_t)G;
+        const uint32_t nb = L.nb, nops = nb * (uint32_t)S;
         uint64_t *so = reinterpret_cast<uint64_t *>(smem + staged);
         uint32_t *sw = reinterpret_cast<uint32_t *>(so + nops);
         for (uint32_t i = t; i < nops; i += 32) so[i] = L.b_ops[i];
@@ -622,6 +631,16 @@ __global__ void __launch_bounds__(32) k_traj_g(const TrajLaunch L, uint32_t stag
         b_arg = sw + nb;
         b_match = reinterpret_cast<const int32_t *>(sw + 2 * nb);
         if (kons) kons = sk;
+    }
+    // the cooperative groups' scratch (coop.cuh), zeroed once
+    [[maybe_unused]] uint32_t *sb = nullptr;
+    [[maybe_unused]] coop::Group grp;
+    if constexpr (COOP) {
+        constexpr int SW = coop::scratch_words<W>();
+        coop::zero_scratch(smem + coop_at, (32 / W) * SW, t);
+        sb = smem + coop_at + (t / W) * SW;
+        grp = coop::group_of<W>(t);
+        __syncwarp();
     }
     if (have) {
         for (uint32_t sl = g; sl < slots; sl += G) {
@@ -658,14 +677,27 @@ __global__ void __launch_bounds__(32) k_traj_g(const TrajLaunch L, uint32_t stag
         while (b < L.nb) {
             const uint32_t kind = b_ctl[b];
             if (kind == 0u) {                              // micro-operations
-                const uint64_t u = b_ops[(size_t)b * G + g];
+                const uint64_t u = b_ops[(size_t)b * S + slot];
                 uint32_t res[W];
                 int dest = -1;
+                // COOP: the operands of this group's FMA/ADD/SUB/MUL, which
+                // every lane of the warp then computes at once
+                [[maybe_unused]] uint32_t ca[K > 1 ? W : 1], cb[K > 1 ? W : 1], cc[K > 1 ? W : 1];
+                [[maybe_unused]] int cop = 0, crnd = 0;
+                [[maybe_unused]] bool carith = false;
+                if constexpr (COOP) {
+#pragma unroll
+                    for (int w = 0; w < W; w++) ca[w] = cb[w] = cc[w] = 0u;
+                }
                 if (mine && u != ~0ull) {
                     const uint32_t ia = (uint32_t)(u >> 28) & 0xFFFu;
                     if ((u >> 14) & 1u) {                  // MOVE
+                        if constexpr (COOP) {
+                            res[0] = LOC(ia, jw);
+                        } else {
 #pragma unroll
-                        for (int w = 0; w < W; w++) res[w] = LOC(ia, w);
+                            for (int w = 0; w < W; w++) res[w] = LOC(ia, w);
+                        }
                     } else {
                         const uint32_t ib = (uint32_t)(u >> 40) & 0xFFFu, ic = (uint32_t)(u >> 52) & 0xFFFu;
                         const bool ka = (u >> 11) & 1u, kb = (u >> 12) & 1u, kc = (u >> 13) & 1u;
@@ -678,17 +710,61 @@ __global__ void __launch_bounds__(32) k_traj_g(const TrajLaunch L, uint32_t stag
                             vc[w] = kc ? kons[ic * W + w] : LOC(ic, w);
                         }
                         if ((u >> 15) & 1u) vc[W - 1] ^= 0x80000000u;    // a NEG folded into c
-                        // latency form: this warp's lanes wait on each result
-                        if (op <= 3) sf::arith_rt<FMT, true>(op, va, vb, vc, rnd, res, fl);
-                        else sf::simple<FMT>(op, va, vb, vc, res, fl);
-                        flags |= fl;
+                        if constexpr (COOP) {
+                            if (op <= 3) {
+                                carith = true;
+                                cop = op;
+                                crnd = rnd;
+#pragma unroll
+                                for (int w = 0; w < W; w++) {
+                                    ca[w] = va[w];
+                                    cb[w] = vb[w];
+                                    cc[w] = vc[w];
+                                }
+                            } else {
+                                uint32_t full[W];
+                                sf::simple<FMT>(op, va, vb, vc, full, fl);
+                                uint32_t r = 0u;
+#pragma unroll
+                                for (int w = 0; w < W; w++) r = w == jw ? full[w] : r;
+                                res[0] = r;
+                                flags |= fl;
+                            }
+                        } else {
+                            // latency form: this warp's lanes wait on each result
+                            if (op <= 3) sf::arith_rt<FMT, true>(op, va, vb, vc, rnd, res, fl);
+                            else sf::simple<FMT>(op, va, vb, vc, res, fl);
+                            flags |= fl;
+                        }
                     }
                     dest = (int)((u >> 16) & 0xFFFu);
                 }
+                if constexpr (COOP) {
+                    // the warp's groups together (coop.cuh); where a group does
+                    // not take its element, the one-thread code (the same in
+                    // every thread of the group), word jw kept
+                    uint32_t r, fl = 0u;
+                    const bool ok = coop::arith_group<FMT>(grp, cop, ca, cb, cc, crnd, sb, r, fl);
+                    if (carith) {
+                        if (!ok) {
+                            uint32_t full[W];
+                            sf::arith_rt<FMT, true>(cop, ca, cb, cc, crnd, full, fl);
+                            r = 0u;
+#pragma unroll
+                            for (int w = 0; w < W; w++) r = w == jw ? full[w] : r;
+                        }
+                        res[0] = r;
+                        flags |= fl;
+                    }
+                }
                 __syncwarp();
                 if (dest >= 0) {
+                    if constexpr (COOP) {
+                        LOC((uint32_t)dest, jw) = res[0];
+                    } else {
 #pragma unroll
-                    for (int w = 0; w < W; w++) LOC((uint32_t)dest, w) = res[w];
+                        for (int w = 0; w < W; w++) LOC((uint32_t)dest, w) = res[w];
+                    }
                 }
                 __syncwarp();
                 b++;
@@ -874,16 +950,22 @@ static cudaError_t go_traj(const TrajLaunch &L, cudaStream_t s)
     return cudaGetLastError();
 }
 
-template <int FMT>
+template <int FMT, bool COOP>
 static cudaError_t go_traj_g(const TrajLaunch &L, cudaStream_t s)
 {
     constexpr int W = sf::Fmt<FMT>::W;
-    const int LPB = 32 / L.G;
+    const int LPB = 32 / L.G, S = L.G / (COOP ? W : 1);
     size_t need = (size_t)L.nloc * (size_t)(W * LPB + 1) * 4;
-    // the schedule and the constant bank after the locations, 8-byte
-    // aligned, when the block's shared memory stays within 96 KB with them
+    // the cooperative groups' scratch after the locations
+    uint32_t coop_at = 0;
+    if (COOP) {
+        coop_at = (uint32_t)(need / 4);
+        need += (size_t)(32 / W) * coop::scratch_words<W>() * 4;
+    }
+    // the schedule and the constant bank after them, 8-byte aligned, when
+    // the block's shared memory stays within 96 KB with them
     const size_t at = (need + 7) / 8 * 8;
-    const size_t extra = (size_t)L.nb * L.G * 8 + (size_t)L.nb * 12 + (size_t)L.P.n_consts * W * 4;
+    const size_t extra = (size_t)L.nb * S * 8 + (size_t)L.nb * 12 + (size_t)L.P.n_consts * W * 4;
     uint32_t staged = 0;
     if (at + extra <= (96u << 10)) {
         staged = (uint32_t)(at / 4);
@@ -891,17 +973,17 @@ static cudaError_t go_traj_g(const TrajLaunch &L, cudaStream_t s)
     }
     const size_t blocks = (L.n + LPB - 1) / LPB;
     if (L.req_of) {
-        const size_t smem = capped_smem(k_traj_g<FMT, true>, L, 32, need);
+        const size_t smem = capped_smem(k_traj_g<FMT, true, COOP>, L, 32, need);
         static unsigned done = 0;
-        cudaError_t e = smem_ceiling_once(k_traj_g<FMT, true>, done);
+        cudaError_t e = smem_ceiling_once(k_traj_g<FMT, true, COOP>, done);
         if (e != cudaSuccess) return e;
-        k_traj_g<FMT, true><<<(unsigned)blocks, 32, smem, s>>>(L, staged);
+        k_traj_g<FMT, true, COOP><<<(unsigned)blocks, 32, smem, s>>>(L, staged, coop_at);
     } else {
-        const size_t smem = capped_smem(k_traj_g<FMT, false>, L, 32, need);
+        const size_t smem = capped_smem(k_traj_g<FMT, false, COOP>, L, 32, need);
         static unsigned done = 0;
-        cudaError_t e = smem_ceiling_once(k_traj_g<FMT, false>, done);
+        cudaError_t e = smem_ceiling_once(k_traj_g<FMT, false, COOP>, done);
         if (e != cudaSuccess) return e;
-        k_traj_g<FMT, false><<<(unsigned)blocks, 32, smem, s>>>(L, staged);
+        k_traj_g<FMT, false, COOP><<<(unsigned)blocks, 32, smem, s>>>(L, staged, coop_at);
     }
     return cudaGetLastError();
 }
@@ -911,10 +993,10 @@ cudaError_t launch_traj(const TrajLaunch &L, cudaStream_t s)
     if (L.n == 0) return cudaSuccess;
     if (L.G > 1 && L.nb) {
         switch (L.P.fmt) {
-        case 0: return go_traj_g<0>(L, s);
-        case 1: return go_traj_g<1>(L, s);
-        case 2: return go_traj_g<2>(L, s);
-        default: return go_traj_g<3>(L, s);
+        case 0: return go_traj_g<0, false>(L, s);
+        case 1: return go_traj_g<1, false>(L, s);
+        case 2: return L.K > 1 ? go_traj_g<2, true>(L, s) : go_traj_g<2, false>(L, s);
+        default: return L.K > 1 ? go_traj_g<3, true>(L, s) : go_traj_g<3, false>(L, s);
         }
     }
     switch (L.P.fmt) {

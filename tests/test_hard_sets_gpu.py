@@ -139,14 +139,15 @@ def test_mutated_programs_through_the_sequencer_kernel(gpu, oracle):
     assert ran > 150, ran
 
 
-@pytest.mark.parametrize("G", ["1", "8", "32"])
+@pytest.mark.parametrize("G", ["1", "8", "32", "8c", "32c"])
 @pytest.mark.parametrize("key,fmt,slots,base", [("l63", 3, 3, 1.0), ("hh", 3, 4, None),
                                                 ("l96", 2, 40, 8.0)], ids=["l63", "hh", "l96"])
 def test_mutated_ode_programs_through_the_trajectory_kernel(gpu, oracle, monkeypatch, G, key, fmt,
                                                             slots, base):
     import bench_suites as suites
     from test_traj_gpu import _traj
-    monkeypatch.setenv("CFTG_LANE_THREADS", G)
+    monkeypatch.setenv("CFTG_LANE_THREADS", G.rstrip("c"))
+    monkeypatch.setenv("CFTG_LANE_COOP", "1" if G.endswith("c") else "0")
     z = np.load(su.GOLD / "odes.npz")
     img0, bank = z[key + "_image"].copy(), z[key + "_bank"].copy()
     W = wl.words(fmt)

@@ -73,12 +73,14 @@ def test_certificate_segments_as_one_trajectory_launch(gpu):
     assert fl == int(np.bitwise_or.reduce(z["flags"])) and st == 0
 
 
-@pytest.fixture(params=["auto", "1", "2", "4", "32"])
+@pytest.fixture(params=["auto", "1", "2", "4", "32", "8c", "32c"])
 def lane_threads(request, monkeypatch):
     """Threads a lane for the trajectory launches: the planner's choice, or
-    forced (1 = the plain interpreter, else the bundle schedule)."""
+    forced (1 = the plain interpreter, else the bundle schedule; "c": with
+    the cooperative binary128/256 arithmetic, W threads an operation)."""
     if request.param != "auto":
-        monkeypatch.setenv("CFTG_LANE_THREADS", request.param)
+        monkeypatch.setenv("CFTG_LANE_THREADS", request.param.rstrip("c"))
+        monkeypatch.setenv("CFTG_LANE_COOP", "1" if request.param.endswith("c") else "0")
     return request.param
 
 

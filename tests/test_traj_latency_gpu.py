@@ -1,7 +1,7 @@
 """The trajectory kernel's arithmetic (FMA, ADD, SUB, MUL in the latency
 form its bundles use: the split product, selects on the integer ALU, the
-one-test unpack of usual operands) against the oracle's sequencer, element
-by element. Each lane runs a one-operation program once, so every lane is
+one-test unpack of usual operands; and the cooperative form, W threads an
+operation) against the oracle's sequencer, element by element. Each lane runs a one-operation program once, so every lane is
 one element: every format x operation x rounding attribute, over the
 benchmark's operand mix, rows that are all hard cases (exact cancellations,
 ties) and, at binary32/64, operands aimed at the rounding edges (results
@@ -95,9 +95,12 @@ def operand_sets(fmt, n):
     return [tuple(np.ascontiguousarray(x, np.uint32) for x in s) for s in sets]
 
 
-@pytest.fixture(params=["2", "8"])
+@pytest.fixture(params=["2", "8", "8c", "32c"])
 def lane_threads(request, monkeypatch):
-    monkeypatch.setenv("CFTG_LANE_THREADS", request.param)
+    """Threads a lane, "c": the cooperative arithmetic (W threads an
+    operation at binary128/256; the one-thread form at binary32/64)."""
+    monkeypatch.setenv("CFTG_LANE_THREADS", request.param.rstrip("c"))
+    monkeypatch.setenv("CFTG_LANE_COOP", "1" if request.param.endswith("c") else "0")
     return request.param
 
 
