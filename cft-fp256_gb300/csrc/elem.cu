@@ -10,8 +10,16 @@
 
 namespace cftg {
 
+// Blocks of 256 an SM the compiler is asked to fit (registers a thread
+// at most 65,536 / (256 x blocks)): binary256 FMA at five (48 registers, a
+// few spilled, against 64 and four blocks unasked) gives its warps' memory
+// and integer latencies more company (warps active 43 -> 51 %; 31.9 -> 32.1
+// Gelem/s at n = 2^24).
 template <int FMT, int KIND>
-__global__ void __launch_bounds__(256) k_elem(const ElemLaunch L)
+__host__ __device__ constexpr int elem_min_blocks() { return FMT == 3 && KIND == K_FMA ? 5 : 1; }
+
+template <int FMT, int KIND>
+__global__ void __launch_bounds__(256, elem_min_blocks<FMT, KIND>()) k_elem(const ElemLaunch L)
 {
     constexpr int W = sf::Fmt<FMT>::W;
     uint32_t acc = 0u;

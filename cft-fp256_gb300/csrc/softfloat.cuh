@@ -315,7 +315,7 @@ enum { OP_FMA = 0, OP_ADD = 1, OP_SUB = 2, OP_MUL = 3 };
 // LAT selects the form for a warp that waits on this one result (a
 // trajectory's dependent chain on a lightly loaded scheduler) rather than
 // for many warps sharing the integer pipes: the product as two independent
-// chains of carry chains (mul_ptx_split), and the selects, the alignment
+// column sums (mul_ptx_split), and the selects, the alignment
 // shift and the complement as selects and XORs on the integer ALU pipe
 // (one instruction a word) instead of multiply-adds (two a word on the
 // IMAD pipe, which balance the pipes under load but lengthen a lone
