@@ -449,11 +449,15 @@ void plan_lanes(cft_program *prog, size_t n, TrajLaunch &L)
     int bestG = 1, bestK = 1;
     // a forced G takes its first candidate, and the cooperative one instead
     // only when it is estimated cheaper (or forced too)
+    // the block's shared memory (seq.cu go_traj_g): the lanes' locations and
+    // the constants as further locations (whose indices must fit the
+    // micro-operation's 12-bit fields), the cooperative scratch, the schedule
     auto consider = [&](int G, int K, double cost) {
         const DevBundles *d = program_bundles(prog, G / K);
-        if (!d) return;
-        size_t bytes = (size_t)d->nloc * (size_t)(W * (32 / G) + 1) * 4;
+        if (!d || d->nloc + L.P.n_consts > 4096u) return;
+        size_t bytes = (size_t)(d->nloc + L.P.n_consts) * (size_t)(W * (32 / G) + 1) * 4;
         if (K > 1) bytes += (size_t)(32 / W) * (size_t)(9 * W) * 4;
+        bytes = (bytes + 7) / 8 * 8 + (size_t)d->nb * (size_t)(G / K) * 8 + (size_t)d->nb * 12;
         if (bytes > (200u << 10)) return;
         const double est = d->weighted * cost * contention(G);
         if ((forced && bestG != G) || est < best) {

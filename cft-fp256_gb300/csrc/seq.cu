@@ -605,32 +605,53 @@ __global__ void __launch_bounds__(32) k_traj_g(const TrajLaunch L, uint32_t stag
     auto LOC = [&](uint32_t p, int w) -> uint32_t & { return smem[p * RS + w * LPB + li]; };
     uint32_t *state = static_cast<uint32_t *>(L.state);
     uint32_t *snaps = static_cast<uint32_t *>(L.snaps);
-    const uint32_t *kons = static_cast<const uint32_t *>(P.d_consts);
-    const uint64_t *b_ops = L.b_ops;
-    const uint32_t *b_ctl = L.b_ctl, *b_arg = L.b_arg;
-    const int32_t *b_match = L.b_match;
-    // the schedule and the constants, read at every bundle, into shared
-    // memory after the lane's locations (word offset `staged`; 0: left in
-    // global memory)
-    if (staged) {
+    // The schedule into shared memory at word `staged`, and the constant
+    // bank as locations kloc .. kloc + n_consts - 1 of every lane of the
+    // block (the launch checks that they fit and that the indices stay
+    // within the micro-operation's 12-bit fields): operands are then all
+    // read the one way, and the schedule with shared-memory loads.
+    const uint32_t kloc = L.nloc;
+    const uint64_t *b_ops;
+    const uint32_t *b_ctl, *b_arg;
+    const int32_t *b_match;
+    {
         const uint32_t nb = L.nb, nops = nb * (uint32_t)S;
         uint64_t *so = reinterpret_cast<uint64_t *>(smem + staged);
         uint32_t *sw = reinterpret_cast<uint32_t *>(so + nops);
-        for (uint32_t i = t; i < nops; i += 32) so[i] = L.b_ops[i];
+        for (uint32_t i = t; i < nops; i += 32) {
+            uint64_t u = L.b_ops[i];
+            if (u != ~0ull) {
+                // operand fields a (bits 28-39), b (40-51), c (52-63), read
+                // from the bank when bits 11, 12, 13 are set
+#pragma unroll
+                for (int k = 0; k < 3; k++) {
+                    if ((u >> (11 + k)) & 1u) {
+                        const int at = 28 + 12 * k;
+                        const uint64_t idx = ((u >> at) & 0xFFFu) + kloc;
+                        u = (u & ~(0xFFFull << at) & ~(1ull << (11 + k))) | (idx << at);
+                    }
+                }
+            }
+            so[i] = u;
+        }
         for (uint32_t i = t; i < nb; i += 32) {
             sw[i] = L.b_ctl[i];
             sw[nb + i] = L.b_arg[i];
             sw[2 * nb + i] = (uint32_t)L.b_match[i];
         }
-        uint32_t *sk = sw + 3 * nb;
-        if (kons)
-            for (uint32_t i = t; i < P.n_consts * (uint32_t)W; i += 32) sk[i] = kons[i];
+        const uint32_t *kons = static_cast<const uint32_t *>(P.d_consts);
+        if (kons) {
+            const uint32_t per = (uint32_t)(W * LPB);
+            for (uint32_t i = t; i < P.n_consts * per; i += 32) {
+                const uint32_t k = i / per, r = i - k * per, w = r / (uint32_t)LPB, l = r - w * LPB;
+                smem[(kloc + k) * RS + w * LPB + l] = kons[k * W + w];
+            }
+        }
         __syncwarp();
         b_ops = so;
         b_ctl = sw;
         b_arg = sw + nb;
         b_match = reinterpret_cast<const int32_t *>(sw + 2 * nb);
-        if (kons) kons = sk;
     }
     // the cooperative groups' scratch (coop.cuh), zeroed once
     [[maybe_unused]] uint32_t *sb = nullptr;
@@ -700,14 +721,13 @@ __global__ void __launch_bounds__(32) k_traj_g(const TrajLaunch L, uint32_t stag
                         }
                     } else {
                         const uint32_t ib = (uint32_t)(u >> 40) & 0xFFFu, ic = (uint32_t)(u >> 52) & 0xFFFu;
-                        const bool ka = (u >> 11) & 1u, kb = (u >> 12) & 1u, kc = (u >> 13) & 1u;
                         const int op = (int)(u & 0xFFu), rnd = (int)((u >> 8) & 7u);
                         uint32_t va[W], vb[W], vc[W], fl = 0u;
 #pragma unroll
-                        for (int w = 0; w < W; w++) {
-                            va[w] = ka ? kons[ia * W + w] : LOC(ia, w);
-                            vb[w] = kb ? kons[ib * W + w] : LOC(ib, w);
-                            vc[w] = kc ? kons[ic * W + w] : LOC(ic, w);
+                        for (int w = 0; w < W; w++) {              // constants are locations too
+                            va[w] = LOC(ia, w);
+                            vb[w] = LOC(ib, w);
+                            vc[w] = LOC(ic, w);
                         }
                         if ((u >> 15) & 1u) vc[W - 1] ^= 0x80000000u;    // a NEG folded into c
                         if constexpr (COOP) {
@@ -955,22 +975,18 @@ static cudaError_t go_traj_g(const TrajLaunch &L, cudaStream_t s)
 {
     constexpr int W = sf::Fmt<FMT>::W;
     const int LPB = 32 / L.G, S = L.G / (COOP ? W : 1);
-    size_t need = (size_t)L.nloc * (size_t)(W * LPB + 1) * 4;
-    // the cooperative groups' scratch after the locations
+    // a lane's locations and the constants as further locations, the
+    // cooperative groups' scratch, then the schedule, 8-byte aligned
+    // (traj_g_smem, which the planner checked against its limits)
+    size_t need = (size_t)(L.nloc + L.P.n_consts) * (size_t)(W * LPB + 1) * 4;
     uint32_t coop_at = 0;
     if (COOP) {
         coop_at = (uint32_t)(need / 4);
         need += (size_t)(32 / W) * coop::scratch_words<W>() * 4;
     }
-    // the schedule and the constant bank after them, 8-byte aligned, when
-    // the block's shared memory stays within 96 KB with them
     const size_t at = (need + 7) / 8 * 8;
-    const size_t extra = (size_t)L.nb * S * 8 + (size_t)L.nb * 12 + (size_t)L.P.n_consts * W * 4;
-    uint32_t staged = 0;
-    if (at + extra <= (96u << 10)) {
-        staged = (uint32_t)(at / 4);
-        need = at + extra;
-    }
+    const uint32_t staged = (uint32_t)(at / 4);
+    need = at + (size_t)L.nb * S * 8 + (size_t)L.nb * 12;
     const size_t blocks = (L.n + LPB - 1) / LPB;
     if (L.req_of) {
         const size_t smem = capped_smem(k_traj_g<FMT, true, COOP>, L, 32, need);
