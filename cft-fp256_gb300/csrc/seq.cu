@@ -568,6 +568,47 @@ __global__ void k_traj(const TrajLaunch L, bool scratch_shared)
     }
 }
 
+// The words between one location and the next in a trajectory block's
+// shared memory (k_traj_g): LPB lanes of W words, then a pad of one vector
+// (16 bytes from binary128 up, the element below) so that one lane's
+// different locations start in different banks.
+template <int W>
+__host__ __device__ constexpr int traj_g_stride(int lpb) { return W * lpb + (W >= 4 ? 4 : W); }
+
+// A location's W words as one or two vector loads or stores (the stride
+// keeps every location 16-byte aligned from binary128 up, 8-byte at
+// binary64).
+template <int W>
+SFD void load_loc(const uint32_t *p, uint32_t (&x)[W])
+{
+    if constexpr (W >= 4) {
+#pragma unroll
+        for (int h = 0; h < W / 4; h++) {
+            const uint4 v = reinterpret_cast<const uint4 *>(p)[h];
+            x[4 * h] = v.x; x[4 * h + 1] = v.y; x[4 * h + 2] = v.z; x[4 * h + 3] = v.w;
+        }
+    } else if constexpr (W == 2) {
+        const uint2 v = *reinterpret_cast<const uint2 *>(p);
+        x[0] = v.x; x[1] = v.y;
+    } else {
+        x[0] = p[0];
+    }
+}
+
+template <int W>
+SFD void store_loc(uint32_t *p, const uint32_t (&x)[W])
+{
+    if constexpr (W >= 4) {
+#pragma unroll
+        for (int h = 0; h < W / 4; h++)
+            reinterpret_cast<uint4 *>(p)[h] = make_uint4(x[4 * h], x[4 * h + 1], x[4 * h + 2], x[4 * h + 3]);
+    } else if constexpr (W == 2) {
+        *reinterpret_cast<uint2 *>(p) = make_uint2(x[0], x[1]);
+    } else {
+        p[0] = x[0];
+    }
+}
+
 // Trajectories with G threads a lane through the bundle schedule
 // (bundle.cpp). A block is one warp holding 32/G lanes; the G threads
 // [li*G, li*G + G) serve lane li. A lane's locations (registers 0..31,
@@ -590,7 +631,7 @@ __global__ void __launch_bounds__(32) k_traj_g(const TrajLaunch L, uint32_t stag
 {
     constexpr int W = sf::Fmt<FMT>::W;
     constexpr int K = COOP ? W : 1;                  // threads a micro-operation
-    extern __shared__ uint32_t smem[];
+    extern __shared__ __align__(16) uint32_t smem[];
     const SeqProgram &P = L.P;
     const int G = L.G, LPB = 32 / G, S = G / K;      // S: micro-operations a bundle
     const int t = threadIdx.x, g = t & (G - 1), li = t / G;
@@ -601,8 +642,11 @@ __global__ void __launch_bounds__(32) k_traj_g(const TrajLaunch L, uint32_t stag
     const uint32_t segs = have ? L.segments[lane] : 0u;
     const int nregs = P.nregs > 0 ? (int)P.nregs : 1;
     const uint32_t slots = P.n_scratch_out, reach = P.reach;
-    const int RS = W * LPB + 1;
-    auto LOC = [&](uint32_t p, int w) -> uint32_t & { return smem[p * RS + w * LPB + li]; };
+    // location p of lane li: W consecutive words at p * RS + li * W, so an
+    // operand is one or two vector loads; the pad after each location's LPB
+    // lanes puts the same lane's different locations in different banks
+    const int RS = traj_g_stride<W>(LPB);
+    auto LOC = [&](uint32_t p, int w) -> uint32_t & { return smem[p * RS + li * W + w]; };
     uint32_t *state = static_cast<uint32_t *>(L.state);
     uint32_t *snaps = static_cast<uint32_t *>(L.snaps);
     // The schedule into shared memory at word `staged`, and the constant
@@ -644,7 +688,7 @@ __global__ void __launch_bounds__(32) k_traj_g(const TrajLaunch L, uint32_t stag
             const uint32_t per = (uint32_t)(W * LPB);
             for (uint32_t i = t; i < P.n_consts * per; i += 32) {
                 const uint32_t k = i / per, r = i - k * per, w = r / (uint32_t)LPB, l = r - w * LPB;
-                smem[(kloc + k) * RS + w * LPB + l] = kons[k * W + w];
+                smem[(kloc + k) * RS + l * W + w] = kons[k * W + w];
             }
         }
         __syncwarp();
@@ -713,22 +757,15 @@ __global__ void __launch_bounds__(32) k_traj_g(const TrajLaunch L, uint32_t stag
                 if (mine && u != ~0ull) {
                     const uint32_t ia = (uint32_t)(u >> 28) & 0xFFFu;
                     if ((u >> 14) & 1u) {                  // MOVE
-                        if constexpr (COOP) {
-                            res[0] = LOC(ia, jw);
-                        } else {
-#pragma unroll
-                            for (int w = 0; w < W; w++) res[w] = LOC(ia, w);
-                        }
+                        if constexpr (COOP) res[0] = LOC(ia, jw);
+                        else load_loc<W>(&LOC(ia, 0), res);
                     } else {
                         const uint32_t ib = (uint32_t)(u >> 40) & 0xFFFu, ic = (uint32_t)(u >> 52) & 0xFFFu;
                         const int op = (int)(u & 0xFFu), rnd = (int)((u >> 8) & 7u);
                         uint32_t va[W], vb[W], vc[W], fl = 0u;
-#pragma unroll
-                        for (int w = 0; w < W; w++) {              // constants are locations too
-                            va[w] = LOC(ia, w);
-                            vb[w] = LOC(ib, w);
-                            vc[w] = LOC(ic, w);
-                        }
+                        load_loc<W>(&LOC(ia, 0), va);              // constants are locations too
+                        load_loc<W>(&LOC(ib, 0), vb);
+                        load_loc<W>(&LOC(ic, 0), vc);
                         if ((u >> 15) & 1u) vc[W - 1] ^= 0x80000000u;    // a NEG folded into c
                         if constexpr (COOP) {
                             if (op <= 3) {
@@ -779,12 +816,8 @@ __global__ void __launch_bounds__(32) k_traj_g(const TrajLaunch L, uint32_t stag
                 }
                 __syncwarp();
                 if (dest >= 0) {
-                    if constexpr (COOP) {
-                        LOC((uint32_t)dest, jw) = res[0];
-                    } else {
-#pragma unroll
-                        for (int w = 0; w < W; w++) LOC((uint32_t)dest, w) = res[w];
-                    }
+                    if constexpr (COOP) LOC((uint32_t)dest, jw) = res[0];
+                    else store_loc<W>(&LOC((uint32_t)dest, 0), res);
                 }
                 __syncwarp();
                 b++;
@@ -978,7 +1011,7 @@ static cudaError_t go_traj_g(const TrajLaunch &L, cudaStream_t s)
     // a lane's locations and the constants as further locations, the
     // cooperative groups' scratch, then the schedule, 8-byte aligned
     // (traj_g_smem, which the planner checked against its limits)
-    size_t need = (size_t)(L.nloc + L.P.n_consts) * (size_t)(W * LPB + 1) * 4;
+    size_t need = (size_t)(L.nloc + L.P.n_consts) * (size_t)traj_g_stride<W>(LPB) * 4;
     uint32_t coop_at = 0;
     if (COOP) {
         coop_at = (uint32_t)(need / 4);
