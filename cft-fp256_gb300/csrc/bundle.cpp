@@ -457,7 +457,7 @@ void plan_lanes(cft_program *prog, size_t n, TrajLaunch &L)
         if (!d || d->nloc + L.P.n_consts > 4096u) return;
         size_t bytes = (size_t)(d->nloc + L.P.n_consts) * (size_t)(W * (32 / G) + (W >= 4 ? 4 : W)) * 4;
         if (K > 1) bytes += (size_t)(32 / W) * (size_t)(9 * W) * 4;
-        bytes = (bytes + 7) / 8 * 8 + (size_t)d->nb * (size_t)(G / K) * 8 + (size_t)d->nb * 12;
+        bytes = (bytes + 7) / 8 * 8 + (size_t)(d->nb + 1) * (size_t)(G / K) * 8 + (size_t)(d->nb + 1) * 12;
         if (bytes > (200u << 10)) return;
         const double est = d->weighted * cost * contention(G);
         if ((forced && bestG != G) || est < best) {

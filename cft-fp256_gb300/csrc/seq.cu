@@ -659,9 +659,17 @@ __global__ void __launch_bounds__(32) k_traj_g(const TrajLaunch L, uint32_t stag
     const uint32_t *b_ctl, *b_arg;
     const int32_t *b_match;
     {
-        const uint32_t nb = L.nb, nops = nb * (uint32_t)S;
+        // one more bundle past the end, a HALT of no-operations, so that the
+        // loop may read the next bundle's words ahead of time
+        const uint32_t nb = L.nb, nops = nb * (uint32_t)S, nb1 = nb + 1;
         uint64_t *so = reinterpret_cast<uint64_t *>(smem + staged);
-        uint32_t *sw = reinterpret_cast<uint32_t *>(so + nops);
+        uint32_t *sw = reinterpret_cast<uint32_t *>(so + nops + S);
+        for (uint32_t i = nops + t; i < nops + S; i += 32) so[i] = ~0ull;
+        if (t == 0) {
+            sw[nb] = 3u;                               // HALT
+            sw[nb1 + nb] = 0u;
+            sw[2 * nb1 + nb] = 0u;
+        }
         for (uint32_t i = t; i < nops; i += 32) {
             uint64_t u = L.b_ops[i];
             if (u != ~0ull) {
@@ -680,8 +688,8 @@ __global__ void __launch_bounds__(32) k_traj_g(const TrajLaunch L, uint32_t stag
         }
         for (uint32_t i = t; i < nb; i += 32) {
             sw[i] = L.b_ctl[i];
-            sw[nb + i] = L.b_arg[i];
-            sw[2 * nb + i] = (uint32_t)L.b_match[i];
+            sw[nb1 + i] = L.b_arg[i];
+            sw[2 * nb1 + i] = (uint32_t)L.b_match[i];
         }
         const uint32_t *kons = static_cast<const uint32_t *>(P.d_consts);
         if (kons) {
@@ -694,8 +702,8 @@ __global__ void __launch_bounds__(32) k_traj_g(const TrajLaunch L, uint32_t stag
         __syncwarp();
         b_ops = so;
         b_ctl = sw;
-        b_arg = sw + nb;
-        b_match = reinterpret_cast<const int32_t *>(sw + 2 * nb);
+        b_arg = sw + nb1;
+        b_match = reinterpret_cast<const int32_t *>(sw + 2 * nb1);
     }
     // the cooperative groups' scratch (coop.cuh), zeroed once
     [[maybe_unused]] uint32_t *sb = nullptr;
@@ -739,10 +747,14 @@ __global__ void __launch_bounds__(32) k_traj_g(const TrajLaunch L, uint32_t stag
         uint32_t body[4], left[4];
         int sp = 0;
         uint32_t b = 0;
+        // this bundle's control word and micro-operation; an operation
+        // bundle reads the next bundle's while it computes
+        uint32_t kind = b_ctl[0];
+        uint64_t u = b_ops[slot];
         while (b < L.nb) {
-            const uint32_t kind = b_ctl[b];
             if (kind == 0u) {                              // micro-operations
-                const uint64_t u = b_ops[(size_t)b * S + slot];
+                const uint32_t kind_next = b_ctl[b + 1];
+                const uint64_t u_next = b_ops[(size_t)(b + 1) * S + slot];
                 uint32_t res[W];
                 int dest = -1;
                 // COOP: the operands of this group's FMA/ADD/SUB/MUL, which
@@ -821,6 +833,9 @@ __global__ void __launch_bounds__(32) k_traj_g(const TrajLaunch L, uint32_t stag
                 }
                 __syncwarp();
                 b++;
+                kind = kind_next;
+                u = u_next;
+                continue;
             } else if (kind == 1u) {                       // REPEAT
                 const bool any = __any_sync(0xFFFFFFFFu, mine);
                 const uint32_t imm = b_arg[b];
@@ -851,6 +866,8 @@ __global__ void __launch_bounds__(32) k_traj_g(const TrajLaunch L, uint32_t stag
             } else {                                       // HALT
                 break;
             }
+            kind = b_ctl[b];
+            u = b_ops[(size_t)b * S + slot];
         }
         __syncwarp();
         if (mine && snaps && L.snap_every && (seg + 1) % L.snap_every == 0) {
@@ -1019,7 +1036,7 @@ static cudaError_t go_traj_g(const TrajLaunch &L, cudaStream_t s)
     }
     const size_t at = (need + 7) / 8 * 8;
     const uint32_t staged = (uint32_t)(at / 4);
-    need = at + (size_t)L.nb * S * 8 + (size_t)L.nb * 12;
+    need = at + (size_t)(L.nb + 1) * S * 8 + (size_t)(L.nb + 1) * 12;   // and a sentinel bundle
     const size_t blocks = (L.n + LPB - 1) / LPB;
     if (L.req_of) {
         const size_t smem = capped_smem(k_traj_g<FMT, true, COOP>, L, 32, need);

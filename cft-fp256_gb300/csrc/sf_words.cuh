@@ -97,6 +97,37 @@ SFD void shr_jam(uint32_t (&x)[N], int s)
     x[0] |= (st != 0u) ? 1u : 0u;
 }
 
+// shl and shr_jam for a lone warp waiting on the result: a shift of less
+// than a word (the usual one: no deep cancellation, an addend of nearly the
+// product's size) by funnel shifts alone, the others through the select
+// network. Per lane, without the network's vote.
+template <int N>
+SFD void shl_small_first(uint32_t (&x)[N], int s)
+{
+    if (s < 32) {
+#pragma unroll
+        for (int i = N - 1; i >= 1; i--) x[i] = __funnelshift_l(x[i - 1], x[i], s);
+        x[0] <<= s;
+    } else {
+        shl(x, s);
+    }
+}
+
+template <int N>
+SFD void shr_jam_small_first(uint32_t (&x)[N], int s)
+{
+    if (s <= 0) return;
+    if (s < 32) {
+        const uint32_t st = x[0] & ((1u << s) - 1u);
+#pragma unroll
+        for (int i = 0; i < N - 1; i++) x[i] = __funnelshift_r(x[i], x[i + 1], s);
+        x[N - 1] >>= s;
+        x[0] |= st ? 1u : 0u;
+    } else {
+        shr_jam(x, s);
+    }
+}
+
 // 32-bit multiply-adds as the IMAD pipe runs them (kept as PTX so that a
 // multiplier known to be 0 or 1 is not turned back into a select).
 SFD uint32_t imul(uint32_t a, uint32_t b)

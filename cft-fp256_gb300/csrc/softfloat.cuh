@@ -209,16 +209,26 @@ SFD void round_pack(int sign, uint32_t (&m)[N], int e, int rnd, uint32_t (&out)[
     }
     // Most results keep their leading bit in the top word or the one below
     // (sums without deep cancellation, quotients, roots): when every lane of
-    // the warp has it there, one clz.
-    const unsigned am = __activemask();
+    // the warp has it there, one clz. LAT: each lane on its own (a vote
+    // costs a lone warp more than the clz it saves).
     int L;
-    if (__all_sync(am, m[N - 1] != 0u)) L = 32 * N - __clz(m[N - 1]);
-    else if (__all_sync(am, m[N - 1] == 0u && m[N - 2] != 0u)) L = 32 * (N - 1) - __clz(m[N - 2]);
-    else L = sfw::bitlen(m);
+    if constexpr (LAT) {
+        if (m[N - 1]) L = 32 * N - __clz(m[N - 1]);
+        else if (m[N - 2]) L = 32 * (N - 1) - __clz(m[N - 2]);
+        else L = sfw::bitlen(m);
+    } else {
+        const unsigned am = __activemask();
+        if (__all_sync(am, m[N - 1] != 0u)) L = 32 * N - __clz(m[N - 1]);
+        else if (__all_sync(am, m[N - 1] == 0u && m[N - 2] != 0u)) L = 32 * (N - 1) - __clz(m[N - 2]);
+        else L = sfw::bitlen(m);
+    }
     const int e_norm = e + L - 1;                 // exponent of the leading bit
     // leading bit to the top; narrow windows shift on the IMAD pipe, wide
-    // ones (whose products already load it) on the integer ALU
+    // ones (whose products already load it) on the integer ALU; LAT: a
+    // shift of less than a word (the usual one) without the select network
+    // and its vote
     if constexpr (N <= 5 && !LAT) sfw::shl_imad(m, 32 * N - L);
+    else if constexpr (LAT) sfw::shl_small_first(m, 32 * N - L);
     else sfw::shl(m, 32 * N - L);
 
     uint32_t kept[W];
@@ -378,7 +388,7 @@ SFD void fma_general(const Unp<FMT> &ua, const Unp<FMT> &ub, const Unp<FMT> &uc,
                 }
             }
         }
-        if constexpr (LAT) sfw::shr_jam(X, pbig ? -delta : delta);
+        if constexpr (LAT) sfw::shr_jam_small_first(X, pbig ? -delta : delta);
         else sfw::shr_jam_imad(X, pbig ? -delta : delta);
         if (!pbig) ew += delta;
         const int s_big = pbig ? sp : sc, s_small = pbig ? sc : sp;
