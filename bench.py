@@ -559,7 +559,8 @@ def main():
     ap.add_argument("--fmt", type=int, default=3, help="format of the headline leg (3 = binary256)")
     ap.add_argument("--op", default="fma", choices=["fma", "add", "mul", "div", "sqrt"],
                     help="operation of the --profile leg")
-    ap.add_argument("--suite", default=None, choices=["uneven", "trajectories", "sweep", "serving", "reduce", "link"],
+    ap.add_argument("--suite", default=None, choices=["uneven", "trajectories", "sweep", "serving", "reduce", "link",
+                                                      "bundles"],
                     help="run one of the secondary configurations instead of the headline")
     args = ap.parse_args()
     if args.impl == "reference":
@@ -588,6 +589,17 @@ def main():
             finally:
                 clk.close()
             res["clocks"] = clk.summary()
+            print(json.dumps(res))
+        elif args.suite == "bundles":
+            clk = Clocks(0, keep=True)
+            try:
+                res = suites.bundles(h, timed=clk)
+            finally:
+                clk.close()
+            res["clocks"] = clk.summary()
+            mhz = res["clocks"].get("sm_mhz") or 0
+            for c in res["cells"]:
+                c["cycles_per_bundle"] = c["ns_per_bundle"] * mhz / 1e3 if mhz else None
             print(json.dumps(res))
         elif args.suite == "uneven":
             clk = Clocks(0, keep=True)

@@ -18,6 +18,10 @@ trajectories  the batched sequencer: 4,096 Lorenz-63 RK4 lanes at
         CUDA graph launch (cftg_traj_group_*). Every 1,000 steps each lane's
         state is kept; its tagged SHA-256 and the final states are returned
         for checking against the oracle run segment by segment.
+
+bundles  what one bundle of a trajectory launch costs: binary256 programs
+        that are one dependent chain of a single operation (FMA, MUL, ADD,
+        SUB, NEG, ABS), 32 lanes at 1, 2 and 8 threads a lane.
 """
 import ctypes
 import hashlib
@@ -350,6 +354,77 @@ def trajectories(h, progs, reps=2, separate=False, timed=None):
 
 SWEEP_OPS = (("add", 0, 1), ("sub", 0, 2), ("mul", 0, 3), ("fma", 0, 0), ("div", 1, 0),
              ("sqrt", 2, 0))
+
+
+BUNDLE_CHAINS = (("fma", "fma r0, r0, r1, r2"), ("mul", "mul r0, r0, r1"),
+                 ("add", "add r0, r0, r2"), ("sub", "sub r0, r0, r2"), ("neg", "neg r0, r0"),
+                 ("abs", "abs r0, r0"))
+
+
+def bundles(h, lanes=32, reps=1000, per_rep=10, threads=(1, 2, 8), timed=None):
+    """What one bundle of a trajectory launch costs: for each operation, a
+    binary256 program that is one dependent chain of it (`per_rep` a REPEAT
+    body, `reps` times; r0 the running value, r1 ~ 0.999, r2 ~ 0.001, so
+    the chain stays normal), run as one trajectory launch of `lanes` lanes
+    at G threads a lane (CFTG_LANE_THREADS), best of three. A chain's
+    operations each take a bundle of their own, so the time over the
+    operations is one bundle's: the operation's latency plus the bundle's
+    own work (a NEG chain's is nearly all the latter)."""
+    import os
+    import torch
+    from cftgb import asm
+    from cftgb import workload as wl
+    L = _lib.lib()
+    _bind_traj(L)
+    vp = ctypes.c_void_p
+    init = np.zeros((lanes * 3, 8), np.uint32)
+    for i in range(lanes):
+        for k, v in enumerate((1.5, 0.9990234375, 0.0009765625)):
+            init[i * 3 + k] = wl.from_int(wl.encode_double(3, v), 8)
+    out = {"suite": "bundles", "lanes": lanes, "ops": reps * per_rep, "cells": []}
+    old = os.environ.get("CFTG_LANE_THREADS")
+    stream = torch.cuda.Stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    import contextlib
+    try:
+        for G in threads:
+            os.environ["CFTG_LANE_THREADS"] = str(G)
+            for name, body in BUNDLE_CHAINS:
+                src = (".format fp256\n.deposits 0\n.scratch in 3\n.scratch out 3\n"
+                       "ldl r0, 0\nldl r1, 1\nldl r2, 2\n"
+                       f"repeat {reps}\n" + "\n".join([body] * per_rep) +
+                       "\nendrep\nstl r0, 0\nstl r1, 1\nstl r2, 2\nhalt\n")
+                img = np.frombuffer(asm.assemble(src), np.uint8).copy()
+                prog = vp()
+                _lib.check(L.cft_program_load(h, img.ctypes.data, img.size, ctypes.byref(prog)),
+                           "cft_program_load")
+                state = torch.from_numpy(init.view(np.int32).copy()).cuda()
+                ta = torch.zeros((lanes, 8), dtype=torch.int32, device="cuda")
+                runs = np.ones(lanes, np.uint32)
+                tr = vp()
+                _lib.check(L.cftg_traj_create(prog, runs.ctypes.data, lanes, ta.data_ptr(), None,
+                                              None, None, state.data_ptr(), None, 0, 0, None,
+                                              ctypes.byref(tr)), "cftg_traj_create")
+                best = 1e9
+                for _ in range(3):
+                    state.copy_(torch.from_numpy(init.view(np.int32)).cuda())
+                    torch.cuda.synchronize()
+                    with (timed if timed is not None else contextlib.nullcontext()):
+                        e0.record(stream)
+                        _lib.check(L.cftg_traj_launch(tr, stream.cuda_stream), "cftg_traj_launch")
+                        e1.record(stream)
+                        stream.synchronize()
+                    best = min(best, e0.elapsed_time(e1) / 1e3)
+                L.cftg_traj_free(tr)
+                L.cft_program_free(prog)
+                out["cells"].append({"G": G, "op": name, "s": best,
+                                     "ns_per_bundle": best / (reps * per_rep) * 1e9})
+    finally:
+        if old is None:
+            os.environ.pop("CFTG_LANE_THREADS", None)
+        else:
+            os.environ["CFTG_LANE_THREADS"] = old
+    return out
 
 
 def sweep(h, n=1 << 24, reps=3, seed=11, check=None, spread=1 << 20, timed=None):

@@ -388,7 +388,9 @@ SFD void fma_general(const Unp<FMT> &ua, const Unp<FMT> &ub, const Unp<FMT> &uc,
                 }
             }
         }
-        if constexpr (LAT) sfw::shr_jam_small_first(X, pbig ? -delta : delta);
+        // LAT: a zero addend (every MUL through the run-time dispatch) is
+        // already aligned - it is all zero - so its shift is skipped
+        if constexpr (LAT) sfw::shr_jam_small_first(X, czero ? 0 : (pbig ? -delta : delta));
         else sfw::shr_jam_imad(X, pbig ? -delta : delta);
         if (!pbig) ew += delta;
         const int s_big = pbig ? sp : sc, s_small = pbig ? sc : sp;
