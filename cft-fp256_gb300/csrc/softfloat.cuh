@@ -163,6 +163,20 @@ SFD bool round_up(int rnd, int sign, bool guard, bool sticky, bool lsb)
     }
 }
 
+// round_up by selects: a warp whose lanes round under different attributes
+// (a trajectory's bundle) takes no branch
+SFD bool round_up_sel(int rnd, int sign, bool guard, bool sticky, bool lsb)
+{
+    const bool gs = guard || sticky;
+    bool r = false;                                           // RTZ
+    r = rnd == RNE ? (guard && (sticky || lsb)) : r;
+    r = rnd == RDN ? (sign && gs) : r;
+    r = rnd == RUP ? (!sign && gs) : r;
+    r = rnd == RTTZ ? (guard && sticky) : r;
+    r = rnd == RMM ? guard : r;
+    return r;
+}
+
 SFD bool overflow_to_inf(int rnd, int sign)
 {
     return rnd == RTZ ? false : rnd == RDN ? (sign != 0) : rnd == RUP ? (sign == 0) : true;
@@ -234,7 +248,8 @@ SFD void round_pack(int sign, uint32_t (&m)[N], int e, int rnd, uint32_t (&out)[
     uint32_t kept[W];
     bool guard, sticky;
     take_top<FMT, N>(m, kept, guard, sticky);
-    bool up = round_up(rnd, sign, guard, sticky, kept[0] & 1u);
+    bool up = LAT ? round_up_sel(rnd, sign, guard, sticky, kept[0] & 1u)
+                  : round_up(rnd, sign, guard, sticky, kept[0] & 1u);
 
     const int d = F::EMIN - e_norm;              // > 0: below the normal range
     bool carry_unb = false;
@@ -251,7 +266,13 @@ SFD void round_pack(int sign, uint32_t (&m)[N], int e, int rnd, uint32_t (&out)[
     }
     const bool inexact = guard || sticky;
     uint32_t fl = inexact ? F_INEXACT : 0u;
-    if (up) {
+    if constexpr (LAT && W >= 2) {
+        // the increment as a carry chain with up as its carry in, no branch
+        uint32_t zw[W];
+#pragma unroll
+        for (int i = 0; i < W; i++) zw[i] = 0u;
+        sfw::AddPtx<W>::add(kept, zw, up ? 1u : 0u);
+    } else if (up) {
         if constexpr (W >= 2) sfw::IncPtx<W>::inc(kept);
         else sfw::inc(kept);
     }
@@ -408,8 +429,8 @@ SFD void fma_general(const Unp<FMT> &ua, const Unp<FMT> &ub, const Unp<FMT> &uc,
         const bool neg = sub && !cy;               // Y < X: the result is X - Y
         // the negation only where some lane of the warp needs it (the
         // smaller-exponent term is the larger magnitude only under deep
-        // cancellation)
-        if (__any_sync(__activemask(), neg)) {
+        // cancellation); LAT: where this lane needs it, without the vote
+        if (LAT ? neg : __any_sync(__activemask(), neg)) {
             const uint32_t m2 = neg ? 0xFFFFFFFFu : 0u;
             uint32_t z[N];
 #pragma unroll
