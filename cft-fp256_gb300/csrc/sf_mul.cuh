@@ -52,6 +52,23 @@ template <> struct MulPtx<8> {
     }
 };
 
+// r (N + 1 words) = a * b (N words): each word's 64-bit product plus the
+// carry from the word below, one wide multiply-add a word (the low half is
+// the word, the high half the next carry), in place of MulPtx::row's two
+// carry chains of halves.
+template <int N>
+__device__ __forceinline__ void mul_row_wide(uint32_t (&r)[N + 1], uint32_t a, const uint32_t (&b)[N])
+{
+    uint32_t c = 0u;
+#pragma unroll
+    for (int j = 0; j < N; j++) {
+        const uint64_t t = (uint64_t)a * b[j] + c;
+        r[j] = (uint32_t)t;
+        c = (uint32_t)(t >> 32);
+    }
+    r[N] = c;
+}
+
 // u (K words) -= t (K words); returns the borrow out (1 when u < t). One
 // borrow chain; K = N + 1 for the division's multiply-subtract.
 template <int K> struct SubPtx;

@@ -684,11 +684,17 @@ SFD void divrem_top(const uint32_t (&X)[W], const uint32_t (&Y)[W], uint32_t (&q
                     rhat += vt;
                 }
             }
-            // u[j .. j+n] -= qd * Y: the row on the IMAD pipe, one borrow chain
+            // u[j .. j+n] -= qd * Y: the row by wide multiply-adds, one borrow chain
+            // (binary256 keeps the two carry chains of halves: its wide row
+            // took 70 registers against 48 and measured 2 % slower)
             uint32_t row[n + 1];
+            if constexpr (n <= 4) {
+                sfw::mul_row_wide<n>(row, qd, Y);
+            } else {
 #pragma unroll
-            for (int i = 0; i <= n; i++) row[i] = 0u;
-            sfw::MulPtx<n>::row(row, qd, Y);
+                for (int i = 0; i <= n; i++) row[i] = 0u;
+                sfw::MulPtx<n>::row(row, qd, Y);
+            }
             if (sfw::SubPtx<n + 1>::sub(u + j, row)) {   // one too large: add Y back
                 qd--;
                 uint32_t c = 0u;
@@ -825,11 +831,9 @@ SFD void isqrtrem(const uint32_t (&N)[2 * W], uint32_t (&S)[W], uint32_t &rnz)
             D[j] = __funnelshift_l(lo, hi, 1);
         }
         // rem -= D * d   (D * d < B^(i+3) <= B^RW: no carry out, so the
-        // row's top word is zero): the row on the IMAD pipe, one borrow chain
+        // row's top word is zero): the row by wide multiply-adds, one borrow chain
         uint32_t row[RW + 1];
-#pragma unroll
-        for (int j = 0; j <= RW; j++) row[j] = 0u;
-        sfw::MulPtx<RW>::row(row, d, D);
+        sfw::mul_row_wide<RW>(row, d, D);
         // the estimate is never low and at most three high: while rem < 0,
         // d -= 1 and rem += 2 r B + 2 d + 1
         bool neg = sfw::SubPtx<RW>::sub(rem, row) != 0u;
