@@ -612,11 +612,14 @@ SFD void store_loc(uint32_t *p, const uint32_t (&x)[W])
 // Trajectories with G threads a lane through the bundle schedule
 // (bundle.cpp). A block is one warp holding 32/G lanes; the G threads
 // [li*G, li*G + G) serve lane li. A lane's locations (registers 0..31,
-// scratch slots 32.., renamed values after them) live in shared memory,
-// [(p*W + w)*LPB + li] with one pad word a location so that the group's
-// threads, touching different locations, hit different banks. Each bundle:
-// every thread reads its micro-operation's operands and computes, the warp
-// meets, every thread writes its result, the warp meets again. Only
+// scratch slots 32.., renamed values after them, then the constant bank)
+// live in shared memory, location p of lane li at [p*RS + li*W] with RS a
+// location's LPB lanes plus a pad (traj_g_stride), so that an operand is
+// one or two vector loads and the group's threads, touching different
+// locations, hit different banks. Each bundle: every thread reads its
+// micro-operation's operands and computes, the warp meets, every thread
+// writes its result, the warp meets again; the next bundle's control word
+// and micro-operation are read while this one computes. Only
 // programs without deposits, lane-mask changes, indexed scratch, quiet
 // regions or raises are scheduled, so the lane byte holds the IEEE flags
 // alone and STATUS stays 0.
