@@ -1,8 +1,10 @@
 // sf_mul.cuh - the significand product on the IMAD pipe.
 //
-// mul_ptx: product scanning (columns), below. MulPtx::row, the row of
-// operand scanning that the split product and the division's
-// multiply-subtract use: r (2N words) = a * b (N words each), for each word
+// mul_ptx and mul_ptx_split: product scanning (columns), below;
+// mul_row_wide: one word times N words by wide multiply-adds (the square
+// root's and the narrow divisions' multiply-subtract). MulPtx::row, the row
+// of operand scanning that binary256 division's multiply-subtract uses:
+// r (2N words) = a * b (N words each), for each word
 // a[i], one carry chain adds the low halves of a[i]*b[j] into r[i..i+N]
 // (mad.lo.cc / madc.lo.cc, then addc into r[i+N]) and a second adds the
 // high halves into r[i+1..i+N] (mad.hi.cc / madc.hi.cc). After rows 0..i
