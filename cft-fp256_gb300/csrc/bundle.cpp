@@ -419,16 +419,31 @@ namespace cftg {
 
 // Choose the threads a lane for a trajectory launch of n lanes: the G whose
 // schedule steps through the fewest bundles a run, weighed by how many warps
-// then share a scheduler (152 SMs x 4), with a bundle counted a quarter
-// dearer than one instruction of the plain interpreter (two warp barriers,
-// operands read from shared memory). G = 1 keeps the plain interpreter.
+// then share a scheduler (152 SMs x 4) and by how many lanes share a warp,
+// with a bundle counted a quarter dearer than one instruction of the plain
+// interpreter (two warp barriers, operands read from shared memory). G = 1
+// keeps the plain interpreter.
+//  * Sharing a scheduler: with the lanes' run counts (runs_desc, longest
+//    first as the launch places them), the warps' lengths summed over the
+//    longest one's - the warps that are still running, on average, while
+//    the longest lane runs - over the schedulers; without them, all the
+//    warps over the schedulers.
+//  * Sharing a warp: a warp's lanes take their own branches through each
+//    operation and the warp runs them all, a bundle costing 4 % more for
+//    each lane past the first (measured on Lorenz-63's configuration at
+//    binary256: 16 threads a lane ran its 4,096 lanes in 1.34 s, 8 threads
+//    a lane in 1.45 s, at the same 13 bundles a step). Counted for the
+//    launches that give their run counts (cftg_traj_create); the serving
+//    loop's batches, which share the GPU with element batches, keep the
+//    plain count (there more threads a lane lengthened program requests'
+//    latency: p50 33 -> 39 ms).
 // Binary128/256 programs may also take the cooperative arithmetic
 // (coop.cuh): W threads a micro-operation, so G threads hold G/W of them a
 // bundle, a bundle counted at COOP_BUNDLE instead; only when
 // CFTG_LANE_COOP=1 asks for it (see below). CFTG_LANE_THREADS forces G.
-void plan_lanes(cft_program *prog, size_t n, TrajLaunch &L)
+void plan_lanes(cft_program *prog, size_t n, TrajLaunch &L, const uint32_t *runs_desc)
 {
-    constexpr double PLAIN_BUNDLE = 1.25, COOP_BUNDLE = 0.8;
+    constexpr double PLAIN_BUNDLE = 1.25, COOP_BUNDLE = 0.8, LANE_DIVERGENCE = 0.04;
     L.G = 1;
     L.K = 1;
     L.nb = 0;
@@ -439,7 +454,16 @@ void plan_lanes(cft_program *prog, size_t n, TrajLaunch &L)
     const int coop_mode = cenv ? atoi(cenv) : 0;
     const double slots = (double)sm_count() * 4.0;
     auto contention = [&](int G) {
-        const double warps = std::ceil((double)n * G / 32.0);
+        double warps;
+        if (runs_desc && runs_desc[0]) {
+            // warp w holds lanes [w*LPB, w*LPB + LPB), the longest of them first
+            const size_t lpb = (size_t)(32 / G > 0 ? 32 / G : 1);
+            double sum = 0;
+            for (size_t w = 0; w * lpb < n; w++) sum += (double)runs_desc[w * lpb];
+            warps = sum / (double)runs_desc[0];
+        } else {
+            warps = std::ceil((double)n * G / 32.0);
+        }
         return warps > slots ? warps / slots : 1.0;
     };
     const DevBundles *one = program_bundles(prog, 1);
@@ -459,7 +483,8 @@ void plan_lanes(cft_program *prog, size_t n, TrajLaunch &L)
         if (K > 1) bytes += (size_t)(32 / W) * (size_t)(9 * W) * 4;
         bytes = (bytes + 7) / 8 * 8 + (size_t)(d->nb + 1) * (size_t)(G / K) * 8 + (size_t)(d->nb + 1) * 12;
         if (bytes > (200u << 10)) return;
-        const double est = d->weighted * cost * contention(G);
+        const double est = d->weighted * cost * contention(G) *
+                           (runs_desc ? 1.0 + LANE_DIVERGENCE * (double)(32 / G - 1) : 1.0);
         if ((forced && bestG != G) || est < best) {
             best = est;
             bestG = G;

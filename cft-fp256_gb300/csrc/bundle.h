@@ -54,5 +54,8 @@ namespace cftg {
 struct TrajLaunch;
 const DevBundles *program_bundles(cft_program *pr, int G);
 // Sets L.G and the schedule for a launch of n lanes (G = 1: plain).
-void plan_lanes(cft_program *prog, size_t n, TrajLaunch &L);
+// runs_desc (optional): the lanes' run counts, longest first, in the
+// order the launch places lanes (traj.cpp), for the estimate of how many
+// warps share a scheduler over the longest lane's life.
+void plan_lanes(cft_program *prog, size_t n, TrajLaunch &L, const uint32_t *runs_desc = nullptr);
 }

@@ -117,7 +117,9 @@ extern "C" cft_status cftg_traj_create(cft_program *prog, const uint32_t *segmen
     L.scratch = t->d_scratch;
     L.lane_flags = d_lane_flags;
     L.word = t->d_word;
-    plan_lanes(prog, n, L);
+    std::vector<uint32_t> runs_desc(n);
+    for (size_t i = 0; i < n; i++) runs_desc[i] = segments[order[i]];
+    plan_lanes(prog, n, L, n ? runs_desc.data() : nullptr);
     *out = t;
     return CFT_OK;
 }
