@@ -14,9 +14,15 @@ namespace cftg {
 // at most 65,536 / (256 x blocks)): binary256 FMA at five (48 registers, a
 // few spilled, against 64 and four blocks unasked) gives its warps' memory
 // and integer latencies more company (warps active 43 -> 51 %; 31.9 -> 32.1
-// Gelem/s at n = 2^24).
+// Gelem/s at n = 2^24); binary128 FMA, ADD and SUB at six (40 registers,
+// none spilled, against 50 and five): FMA 48.8 -> 49.7, ADD 64.2 -> 65.9.
 template <int FMT, int KIND>
-__host__ __device__ constexpr int elem_min_blocks() { return FMT == 3 && KIND == K_FMA ? 5 : 1; }
+__host__ __device__ constexpr int elem_min_blocks()
+{
+    return FMT == 3 && KIND == K_FMA ? 5
+         : FMT == 2 && (KIND == K_FMA || KIND == K_ADD || KIND == K_SUB) ? 6
+         : 1;
+}
 
 template <int FMT, int KIND>
 __global__ void __launch_bounds__(256, elem_min_blocks<FMT, KIND>()) k_elem(const ElemLaunch L)
@@ -58,6 +64,9 @@ template <int FMT, int KIND>
 static cudaError_t go(const ElemLaunch &L, cudaStream_t s)
 {
     constexpr int T = 256;
+    // eight blocks an SM: more than fit at once, so blocks that start late
+    // fill the SMs whose first blocks finish early (one wave of exactly the
+    // resident blocks measured 3-5 % slower in every cell)
     const size_t want = (L.n + T - 1) / T;
     const size_t cap = (size_t)sm_count() * (L.blocks_per_sm ? L.blocks_per_sm : 8u);
     const unsigned blocks = (unsigned)(want < cap ? want : cap);
