@@ -43,8 +43,12 @@ __global__ void __launch_bounds__(256, elem_min_blocks<FMT, KIND>()) k_elem(cons
         if (L.lane_flags) L.lane_flags[i] = (uint8_t)fl;
         acc |= fl;
     }
+    // the call's flag word: an atomic OR only for bits not already there
+    // (the word fills within the first warps; an OR of thousands of warps
+    // into one word otherwise queues at the L2's atomic unit). A bit read
+    // stale costs a redundant OR, never a lost one.
     acc = __reduce_or_sync(0xFFFFFFFFu, acc);
-    if ((threadIdx.x & 31) == 0 && acc) atomicOr(L.flags, acc);
+    if ((threadIdx.x & 31) == 0 && acc && (acc & ~__ldcg(L.flags))) atomicOr(L.flags, acc);
 }
 
 static int g_sms = 0;
@@ -64,11 +68,14 @@ template <int FMT, int KIND>
 static cudaError_t go(const ElemLaunch &L, cudaStream_t s)
 {
     constexpr int T = 256;
-    // eight blocks an SM: more than fit at once, so blocks that start late
-    // fill the SMs whose first blocks finish early (one wave of exactly the
-    // resident blocks measured 3-5 % slower in every cell)
+    // 64 blocks an SM, many more than fit at once: blocks that start late
+    // fill the SMs whose earlier blocks finish early. Measured at n = 2^24
+    // (binary256 / binary128 FMA, Gelem/s): one wave of exactly the resident
+    // blocks 31.0 / 48.5, 8 an SM 32.0 / 50.7, 16 33.3 / 53.3, 64 33.8 /
+    // 55.0, 256 33.9 / 53.9 (with the flag word's atomics skipped once set;
+    // 22.1 / 31.3 without)
     const size_t want = (L.n + T - 1) / T;
-    const size_t cap = (size_t)sm_count() * (L.blocks_per_sm ? L.blocks_per_sm : 8u);
+    const size_t cap = (size_t)sm_count() * (L.blocks_per_sm ? L.blocks_per_sm : 64u);
     const unsigned blocks = (unsigned)(want < cap ? want : cap);
     k_elem<FMT, KIND><<<blocks ? blocks : 1, T, 0, s>>>(L);
     return cudaGetLastError();
