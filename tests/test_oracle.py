@@ -46,7 +46,7 @@ def _ref():
 @pytest.mark.parametrize("fmt", [0, 1, 2, 3])
 def test_oracle_matches_reference_library(oracle, fmt):
     """Whole arrays, every opcode and mode: values and the OR of the flags;
-    then per element through n=1 calls on a slice."""
+    then every element's own flags through n=1 calls."""
     L, dev = _ref()
     n = 2000
     a, b, c = wl.gen_operands(fmt, n, 77 + fmt, ties=True, triples_frac=0.05)
@@ -69,8 +69,8 @@ def test_oracle_matches_reference_library(oracle, fmt):
                 assert st == 0
                 assert np.array_equal(d, ref), (kind, op, rnd)
                 assert acc == fl.value, (kind, op, rnd)
-                # per-element flags on a slice
-                for i in range(0, n, 97):
+                # every element's flags through n=1 calls
+                for i in range(n):
                     one = np.zeros((1, a.shape[1]), np.uint32)
                     f1 = ctypes.c_uint32()
                     if kind == 0:
@@ -124,8 +124,8 @@ def _raw_and_boundary(fmt, n, seed):
 @pytest.mark.parametrize("fmt", [0, 1, 2, 3])
 def test_oracle_matches_reference_on_raw_encodings(oracle, fmt):
     """FMA/ADD/SUB/MUL, division and square root under every attribute over
-    raw and boundary encodings: the same values and, element by element on a
-    slice, the same flags as the reference library."""
+    raw and boundary encodings: the same values and, element by element, the
+    same flags as the reference library."""
     L, dev = _ref()
     n = 1500
     a, b, c = _raw_and_boundary(fmt, n, 31 + fmt)
@@ -147,7 +147,7 @@ def test_oracle_matches_reference_on_raw_encodings(oracle, fmt):
             bad = np.nonzero((d != ref).any(1))[0]
             assert bad.size == 0, (kind, op, rnd, bad[:5])
             assert acc == fl.value, (kind, op, rnd)
-            for i in range(0, n, 53):
+            for i in range(n):
                 one = np.zeros((1, a.shape[1]), np.uint32)
                 f1 = ctypes.c_uint32()
                 if kind == 0:
